@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the fused per-RK-stage isothermal hydro right-hand side on GB300.
+
+Workload (one "step" = one evolve_isothermal cycle: CFL dt + 3 fused RK3
+stages): the tanh Kelvin-Helmholtz layer with a tracer, 4096 x 4096 cells,
+4 variables (rho, rho vx, rho vy, rho s), PPM4 + Roe, RK3, CFL 0.4, float64
+state. The same workload in float32 is reported under "fp32". Synthetic
+initial data; the state (537 MB in float64) is larger than the 129 MB L2, so
+no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0. With N > 1 (torchrun) every rank advances its
+own independent copy of the workload (replicas, no collective on the data
+path) and the value is the sum over ranks.
+"""
+
+import argparse
+import csv
+import io
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s"
+WORKLOAD = "kelvin_helmholtz_tanh 4096x4096, 4 vars, ppm4+roe, rk3, cfl 0.4"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+# ncu-measured DRAM bytes per cell for one launch of the fused stage kernel
+# (stage 2 of RK3, ppm4+roe, 4 variables), from the capture summarised in
+# profiles/; None until such a capture exists for the dtype.
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": None, "f32": None}
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    p.add_argument("--n", type=int, default=4096, help="grid side (default 4096)")
+    p.add_argument("--no-fp32", action="store_true", help="skip the float32 line")
+    p.add_argument("--cpu-sample", type=int, default=512, help="grid side of the CPU sample")
+    p.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU sample")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# Distributed plumbing (replicas only).
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region.
+# ---------------------------------------------------------------------------
+QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = None
+        if shutil.which("nvidia-smi") is None:
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.handle = open(self.path, "w")
+        self.proc = subprocess.Popen(
+            ["nvidia-smi", f"--query-gpu={QUERY}", "--format=csv,noheader,nounits", "-lms", "200",
+             "-i", str(gpu_index)], stdout=self.handle, stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.handle.close()
+        rows = list(csv.reader(io.StringIO(Path(self.path).read_text())))
+        os.unlink(self.path)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for row in rows:
+            row = [c.strip() for c in row]
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                smax.append(float(row[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, row[5:9]):
+                if flag.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def nvidia_smi_index(local_rank):
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if visible:
+        entries = [v for v in visible.split(",") if v.strip()]
+        if local_rank < len(entries) and entries[local_rank].strip().isdigit():
+            return int(entries[local_rank])
+    return local_rank
+
+
+# ---------------------------------------------------------------------------
+# Our arm.
+# ---------------------------------------------------------------------------
+def fma_peak_tflops(torch, _lib, dtype_id):
+    """Measured FMA throughput (TFLOP/s) of the FP64 or FP32 pipe, all SMs busy."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 8, 4096 if dtype_id == _lib.JX_F64 else 65536
+    sink = torch.zeros(blocks, dtype=torch.float64, device="cuda")
+    stream = _lib.stream_handle()
+    for _ in range(2):
+        _lib.call("jx_probe_fma", dtype_id, blocks, iters, _lib.ptr(sink), stream)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(3):
+        start.record()
+        _lib.call("jx_probe_fma", dtype_id, blocks, iters, _lib.ptr(sink), stream)
+        end.record()
+        end.synchronize()
+        ms = start.elapsed_time(end)
+        best = ms if best is None else min(best, ms)
+    flops = 2.0 * 8 * iters * blocks * 256
+    return flops / (best * 1e-3) / 1e12
+
+
+def measured_peaks():
+    if PEAKS.exists():
+        return json.loads(PEAKS.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def flops_per_cell_stage(key):
+    table = json.loads((ROOT / "jathenax_gb300" / "flops.json").read_text())["flops_per_cell_stage"]
+    return table[key]
+
+
+def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
+    """Time K steps of the resident solve; time the stage kernel alone; e2e."""
+    solve = Solve(U0, 1.0 / n, 1.0 / n, 1.0, 1e-10, "rk3", 0.4, 1e30, 2**31 - 1,
+                  reconstruct="ppm4", rsolver="roe", dtype=dtype)
+    solve.capture(1)
+    for _ in range(args.warmup):
+        solve.graph.replay()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(clocks) if clocks is not None else None
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        solve.graph.replay()
+    end.record()
+    torch.cuda.synchronize()
+    clock_info = sampler.stop() if sampler is not None else None
+    barrier(world)
+    ms = max_over_ranks(start.elapsed_time(end), world)
+    cells = n * n
+    value = world * cells * args.steps / (ms * 1e-3)
+    state = solve.state()
+
+    # The dominant kernel alone: stage 2 (blend form) reading A, pointwise S, writing B.
+    solve.A.copy_(solve.S)
+    reps = max(3, min(20, args.steps))
+    solve.enqueue_stage(2, solve.A, solve.S, solve.B)
+    torch.cuda.synchronize()
+    ks, ke = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ks.record()
+    for _ in range(reps):
+        solve.enqueue_stage(2, solve.A, solve.S, solve.B)
+    ke.record()
+    torch.cuda.synchronize()
+    stage_ms = ks.elapsed_time(ke) / reps
+
+    # End to end through the public API: pinned host state in, one cycle, state out.
+    host_in = solve.S.cpu().pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    e2e_steps = max(2, min(args.steps, 10))
+    solve.advance_host(host_in, host_out)
+    torch.cuda.synchronize()
+    barrier(world)
+    es, ee = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    es.record()
+    for _ in range(e2e_steps):
+        solve.advance_host(host_in, host_out)
+    ee.record()
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(es.elapsed_time(ee), world)
+    state_bytes = host_in.numel() * host_in.element_size()
+    return dict(value=value, ms=ms, stage_ms=stage_ms, clocks=clock_info, solve_state=state,
+                e2e=dict(value=world * cells * e2e_steps / (e2e_ms * 1e-3), unit=METRIC,
+                         h2d_bytes_per_step=state_bytes, d2h_bytes_per_step=state_bytes),
+                dt=state.dt)
+
+
+def cpu_baseline_sample(n, steps):
+    """The float64 oracle (NumPy, one thread) on an n x n sample of the workload."""
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from oracle import hydro_oracle as H
+    U = kelvin_helmholtz_tanh(n, n)
+    prev = np.inf
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _, W = H.primitives(U, 1e-10)
+        dt = float(H.timestep(W, 1 / n, 1 / n, 1.0, 0.4, prev, 0.0, 1e30))
+        U = H.step(U, dt, 1 / n, 1 / n, 1.0, 1e-10, "rk3")
+        prev = dt
+    elapsed = time.perf_counter() - t0
+    return dict(value=n * n * steps / elapsed, unit=METRIC, cores=1, kind="port",
+                sample=f"float64 NumPy oracle, kelvin_helmholtz_tanh {n}x{n}, {steps} full RK3 "
+                       f"cycles (dt + 3 stages), single thread", seconds=round(elapsed, 2))
+
+
+def bench_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    from jathenax_gb300 import _lib
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from jathenax_gb300.solver import Solve
+
+    n = args.n
+    U0 = torch.as_tensor(kelvin_helmholtz_tanh(n, n), device="cuda")
+    peaks, peak_kind = measured_peaks()
+    fp64_peak = fma_peak_tflops(torch, _lib, _lib.JX_F64)
+    fp32_peak = fma_peak_tflops(torch, _lib, _lib.JX_F32)
+
+    r64 = run_precision(torch, _lib, Solve, U0, n, torch.float64, args, world,
+                        clocks=nvidia_smi_index(local))
+    r32 = None if args.no_fp32 else run_precision(torch, _lib, Solve, U0, n, torch.float32, args, world)
+
+    cells = n * n
+    fpcs = flops_per_cell_stage("ppm4/roe/nvar4")
+    nvar, w64 = 4, 8
+
+    def roofline(res, w, peak_tflops, key):
+        flops = cells * fpcs / (res["stage_ms"] * 1e-3) / 1e12
+        stage_bytes = 3 * w * nvar * cells  # stage >= 2: read U and V, write U
+        gbs = stage_bytes / (res["stage_ms"] * 1e-3) / 1e9
+        traffic = STAGE_TRAFFIC_BYTES_PER_CELL[key]
+        hbm_peak = peaks["hbm_gbs"]
+        compute_frac = flops / peak_tflops
+        hbm_frac = gbs / hbm_peak
+        bound = "fp64" if key == "f64" else ("fp32" if compute_frac >= hbm_frac else "hbm")
+        out = {"kernel": f"stage_kernel<{'double' if w == 8 else 'float'},ppm4,roe> (RK3 stage 2)",
+               "bound": bound, "achieved": round(flops, 4), "peak": round(peak_tflops, 4),
+               "unit": "TFLOP/s", "frac": round(compute_frac, 4),
+               "peak_source": f"{key.upper()} FMA pipe measured live by jx_probe_fma",
+               "flops_per_cell_stage": fpcs,
+               "traffic": None if traffic is None else traffic * cells,
+               "stage_ms": round(res["stage_ms"], 4),
+               "hbm": {"achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                       "frac": round(hbm_frac, 4), "peak_source": f"hbm_gbs of {peak_kind}",
+                       "bytes_per_launch": stage_bytes}}
+        if bound == "hbm":
+            out.update(achieved=round(gbs, 1), peak=hbm_peak, unit="GB/s", frac=round(hbm_frac, 4),
+                       peak_source=f"hbm_gbs of {peak_kind}")
+        return out
+
+    line = {
+        "metric": METRIC, "value": round(r64["value"], 1), "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(r64["ms"] / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD.replace("4096x4096", f"{n}x{n}"), "nx": n, "ny": n, "nvar": 4,
+                   "reconstruct": "ppm4", "rsolver": "roe", "integrator": "rk3", "cfl": 0.4,
+                   "step": "one evolve cycle: CFL dt + 3 fused RK stages (CUDA graph replay)",
+                   "l2": f"state {cells * 4 * 8 / 1e6:.0f} MB > 129 MB L2 (no flush needed)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roofline(r64, w64, fp64_peak, "f64"),
+        "e2e": r64["e2e"],
+        "gpu_launches": 4 * args.steps,
+        "clocks": r64["clocks"],
+    }
+    if r32 is not None:
+        line["fp32"] = {"value": round(r32["value"], 1), "unit": METRIC,
+                        "ms_per_step": round(r32["ms"] / args.steps, 4), "dtype": "f32",
+                        "roofline": roofline(r32, 4, fp32_peak, "f32"), "e2e": r32["e2e"]}
+        line["gpu_launches"] += 4 * args.steps
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
+    return line
+
+
+def bench_reference(args, world, rank):
+    """The reference algorithm's CPU path (the float64 oracle port) on host cores."""
+    if rank != 0:
+        return None
+    base = cpu_baseline_sample(args.cpu_sample, max(1, min(args.steps, args.cpu_steps)))
+    steps = base.pop("seconds")
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(base["value"], 1), "unit": METRIC,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_side": args.cpu_sample},
+        "cpu_baseline": dict(base),
+        "e2e": {"value": round(base["value"], 1), "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "seconds": steps,
+    }
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        line = bench_reference(args, world, rank)
+    else:
+        line = bench_ours(args, world, rank, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,517 @@
+// C ABI (include/jx.h): argument checks, workspace layout, and the launch
+// sequences of one RK stage, one full step and the forcing passes.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "jx_aux.cuh"
+#include "jx_internal.h"
+
+using namespace jx;
+
+namespace {
+
+thread_local char g_error[512] = "";
+
+jx_status fail(jx_status code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_error, sizeof(g_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+jx_status cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) return fail(JX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return JX_OK;
+}
+
+// hydro.py:20-36 (AthenaK driver.cpp): (gamma0, gamma1, beta, delta or NaN).
+struct RkRow {
+  double g0, g1, beta, delta;
+  bool has_delta;
+};
+const RkRow kRk2[2] = {{0.0, 1.0, 1.0, 0.0, false}, {0.5, 0.5, 0.5, 0.0, false}};
+const RkRow kRk3[3] = {{0.0, 1.0, 1.0, 0.0, false},
+                       {0.25, 0.75, 0.25, 0.0, false},
+                       {2.0 / 3.0, 1.0 / 3.0, 2.0 / 3.0, 0.0, false}};
+const RkRow kRk4[4] = {
+    {0.0, 1.0, 1.193743905974738, 0.0, false},
+    {0.121098479554482, 0.721781678111411, 0.099279895495783, 0.217683334308543, true},
+    {-3.843833699660025, 2.121209265338722, 1.131678018054042, 1.065841341361089, true},
+    {0.546370891121863, 0.198653035682705, 0.310665766509336, 0.0, true}};
+
+const RkRow* rk_rows(int integrator) {
+  return integrator == JX_RK2 ? kRk2 : (integrator == JX_RK3 ? kRk3 : kRk4);
+}
+
+constexpr size_t kSmemLimit = 227 * 1024;
+constexpr size_t kSmemDefaultCap = 112 * 1024;  // keep two CTAs per SM by default
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+bool finite_nonneg(double x) { return isfinite(x) && x >= 0.0; }
+
+jx_status check_desc(const jx_desc* d) {
+  if (!d) return fail(JX_ERR_INVALID, "null descriptor");
+  if (d->ny < 1 || d->nx < 1) return fail(JX_ERR_INVALID, "grid must have at least one cell per axis");
+  if (d->nvar < 3 || d->nvar > 64) return fail(JX_ERR_INVALID, "nvar must be in [3, 64]");
+  if ((int64_t)d->ny * d->nx > ((int64_t)1 << 31) - 1)
+    return fail(JX_ERR_INVALID, "grid larger than 2^31 cells");
+  if (d->dtype != JX_F64 && d->dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", d->dtype);
+  if (d->recon < JX_DC || d->recon > JX_WENOZ) return fail(JX_ERR_UNSUPPORTED, "unknown reconstruction %d", d->recon);
+  if (d->rsolver < JX_LLF || d->rsolver > JX_ROE) return fail(JX_ERR_UNSUPPORTED, "unknown Riemann solver %d", d->rsolver);
+  if (d->integrator < JX_RK2 || d->integrator > JX_RK4)
+    return fail(JX_ERR_UNSUPPORTED, "unknown integrator %d", d->integrator);
+  if (!(isfinite(d->dx) && d->dx > 0 && isfinite(d->dy) && d->dy > 0))
+    return fail(JX_ERR_INVALID, "dx and dy must be finite and positive");
+  if (!(isfinite(d->cs) && d->cs > 0)) return fail(JX_ERR_INVALID, "cs must be finite and positive");
+  if (!isfinite(d->dfloor)) return fail(JX_ERR_INVALID, "dfloor must be finite");
+  if (!finite_nonneg(d->viscosity)) return fail(JX_ERR_INVALID, "viscosity must be finite and nonnegative");
+  if (!finite_nonneg(d->smagorinsky_cs)) return fail(JX_ERR_INVALID, "smagorinsky_cs must be finite and nonnegative");
+  if (!finite_nonneg(d->drag_rate)) return fail(JX_ERR_INVALID, "drag_rate must be finite and nonnegative");
+  if (d->tile_x < 0 || d->tile_y < 0 || d->tile_x > 256 || d->tile_y > 256)
+    return fail(JX_ERR_INVALID, "tile_x/tile_y must be in [0, 256]");
+  return JX_OK;
+}
+
+struct Tile {
+  int tx, ty, tiles_x, tiles_y;
+  size_t smem;
+};
+
+jx_status resolve_tile(const jx_desc* d, Tile* t) {
+  int tx = d->tile_x > 0 ? d->tile_x : 32;
+  int ty = d->tile_y > 0 ? d->tile_y : 16;
+  size_t smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
+  if (d->tile_x == 0 && d->tile_y == 0) {
+    while (smem > kSmemDefaultCap && ty > 4) {
+      ty /= 2;
+      smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
+    }
+    while (smem > kSmemDefaultCap && tx > 8) {
+      tx /= 2;
+      smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
+    }
+  }
+  if (smem > kSmemLimit)
+    return fail(JX_ERR_INVALID, "tile %dx%d needs %zu bytes of shared memory (limit %zu)", tx, ty, smem, kSmemLimit);
+  t->tx = tx;
+  t->ty = ty;
+  t->tiles_x = (d->nx + tx - 1) / tx;
+  t->tiles_y = (d->ny + ty - 1) / ty;
+  t->smem = smem;
+  if ((int64_t)t->tiles_x * t->tiles_y > ((int64_t)1 << 31) - 1) return fail(JX_ERR_INVALID, "too many tiles");
+  return JX_OK;
+}
+
+struct Layout {
+  size_t scal, cfl, p1, p2, box, total;
+};
+
+Layout layout_for(const jx_desc* d, const Tile& t) {
+  Layout L;
+  size_t off = kWsHeader;
+  L.scal = off;
+  off += 256;
+  L.cfl = off;
+  size_t slots = (size_t)t.tiles_x * t.tiles_y;
+  if (slots < (size_t)kCflBlocksMax) slots = kCflBlocksMax;
+  off = align256(off + slots * kCflSlots * sizeof(double));
+  L.p1 = off;
+  off = align256(off + (size_t)kForceBlocksMax * 4 * sizeof(double));
+  L.p2 = off;
+  off = align256(off + (size_t)kForceBlocksMax * 4 * sizeof(double));
+  L.box = off;
+  off = align256(off + (size_t)kForceBlocksMax * d->nvar * sizeof(double));
+  L.total = off;
+  return L;
+}
+
+struct Ws {
+  WsHeader* header;
+  double *scal, *cfl, *p1, *p2, *box;
+};
+
+jx_status bind_ws(const jx_desc* d, const Tile& t, void* ws, size_t bytes, Ws* w) {
+  if (!ws) return fail(JX_ERR_WORKSPACE, "null workspace");
+  if (((uintptr_t)ws & 255) != 0) return fail(JX_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  Layout L = layout_for(d, t);
+  if (bytes < L.total) return fail(JX_ERR_WORKSPACE, "workspace has %zu bytes, needs %zu", bytes, L.total);
+  char* b = static_cast<char*>(ws);
+  w->header = reinterpret_cast<WsHeader*>(b);
+  w->scal = reinterpret_cast<double*>(b + L.scal);
+  w->cfl = reinterpret_cast<double*>(b + L.cfl);
+  w->p1 = reinterpret_cast<double*>(b + L.p1);
+  w->p2 = reinterpret_cast<double*>(b + L.p2);
+  w->box = reinterpret_cast<double*>(b + L.box);
+  return JX_OK;
+}
+
+DtParams dt_params(const jx_desc* d) {
+  DtParams q;
+  q.dx = d->dx;
+  q.dy = d->dy;
+  q.nu = d->viscosity;
+  q.smag_cs = d->smagorinsky_cs;
+  q.smag_c = d->smagorinsky_cs * d->smagorinsky_cs * d->dx * d->dy;
+  q.drag = d->drag_rate;
+  return q;
+}
+
+CflParams cfl_params(const jx_desc* d, const void* X, const jx_clock* clock, const Ws& w) {
+  CflParams q;
+  q.X = X;
+  q.clock = clock;
+  q.partials = w.cfl;
+  q.header = w.header;
+  q.ny = d->ny;
+  q.nx = d->nx;
+  q.nv = d->nvar;
+  q.smag = d->smagorinsky_cs > 0.0;
+  q.cs = d->cs;
+  q.dfloor = d->dfloor;
+  q.inv_dx = 1.0 / d->dx;
+  q.inv_dy = 1.0 / d->dy;
+  q.inv_4dx = 1.0 / (4.0 * d->dx);
+  q.inv_4dy = 1.0 / (4.0 * d->dy);
+  return q;
+}
+
+cudaError_t launch_stage(const jx_desc* d, const StageParams& p, const Tile& t, cudaStream_t s) {
+  dim3 grid((unsigned)((int64_t)t.tiles_x * t.tiles_y));
+  switch (d->recon) {
+    case JX_DC: return launch_stage_dc(d->dtype, d->rsolver, p, grid, t.smem, s);
+    case JX_PLM: return launch_stage_plm(d->dtype, d->rsolver, p, grid, t.smem, s);
+    case JX_PPM4: return launch_stage_ppm4(d->dtype, d->rsolver, p, grid, t.smem, s);
+    case JX_PPMX: return launch_stage_ppmx(d->dtype, d->rsolver, p, grid, t.smem, s);
+    default: return launch_stage_wenoz(d->dtype, d->rsolver, p, grid, t.smem, s);
+  }
+}
+
+jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, const void* U_in,
+                   const void* V_in, void* U_out, void* V_out, const void* tau, int force_follows,
+                   jx_clock* clock, const jx_trace* trace, cudaStream_t s) {
+  const int n = jx_num_stages(d->integrator);
+  if (stage < 1 || stage > n) return fail(JX_ERR_INVALID, "stage %d outside 1..%d", stage, n);
+  if (!U_in || !V_in || !U_out || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
+  const RkRow& row = rk_rows(d->integrator)[stage - 1];
+  if (U_in == U_out || (row.has_delta && U_in == V_out))
+    return fail(JX_ERR_INVALID, "U_in must not alias an output");
+  const bool last = stage == n;
+  StageParams p;
+  memset(&p, 0, sizeof(p));
+  p.U = U_in;
+  p.V = V_in;
+  p.Uout = U_out;
+  p.Vout = row.has_delta ? V_out : nullptr;
+  p.tau = tau;
+  p.clock = clock;
+  p.partials = w.cfl;
+  p.header = w.header;
+  if (trace) p.trace = *trace;
+  p.trace_on = trace != nullptr;
+  p.ny = d->ny;
+  p.nx = d->nx;
+  p.nv = d->nvar;
+  p.tx = t.tx;
+  p.ty = t.ty;
+  p.tiles_x = t.tiles_x;
+  p.dx = d->dx;
+  p.dy = d->dy;
+  p.inv_dx = 1.0 / d->dx;
+  p.inv_dy = 1.0 / d->dy;
+  p.inv_4dx = 1.0 / (4.0 * d->dx);
+  p.inv_4dy = 1.0 / (4.0 * d->dy);
+  p.cs = d->cs;
+  p.dfloor = d->dfloor;
+  p.nu = d->viscosity;
+  p.smag_c = d->smagorinsky_cs * d->smagorinsky_cs * d->dx * d->dy;
+  p.drag = d->drag_rate;
+  p.g0 = row.g0;
+  p.g1 = row.g1;
+  p.beta = row.beta;
+  p.delta = row.delta;
+  p.has_delta = row.has_delta;
+  p.blend = row.g0 != 0.0 && row.g0 + row.g1 == 1.0;  // hydro.py:46
+  p.floor_v = !(d->integrator == JX_RK4 && stage >= 3);  // V is still the floored step-start state
+  p.floor_out = !(last && force_follows);
+  p.want_cfl = last && !force_follows && !(d->smagorinsky_cs > 0.0);
+  p.visc_on = d->viscosity > 0.0 || d->smagorinsky_cs > 0.0;
+  p.smag_on = d->smagorinsky_cs > 0.0;
+  p.drag_on = d->drag_rate > 0.0;
+  return cuda_check(launch_stage(d, p, t, s), "stage kernel");
+}
+
+jx_status do_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock,
+                  const jx_trace* trace, const Ws& w, cudaStream_t s) {
+  if (!f || !f->raw_force) return fail(JX_ERR_INVALID, "forcing needs a raw_force buffer");
+  if (!U || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
+  ForceParams q;
+  memset(&q, 0, sizeof(q));
+  q.clock = clock;
+  q.U = U;
+  q.Uw = U;
+  q.raw = f->raw_force;
+  q.p1 = w.p1;
+  q.p2 = w.p2;
+  q.scal = w.scal;
+  q.partials = w.cfl;
+  q.header = w.header;
+  if (trace) {
+    q.before_kick = trace->before_kick;
+    q.acceleration = trace->acceleration;
+    q.conserved = trace->conserved;
+  }
+  q.ny = d->ny;
+  q.nx = d->nx;
+  q.nv = d->nvar;
+  force_decomposition((int64_t)d->ny * d->nx, &q.nblk, &q.chunk);
+  q.want_cfl = !(d->smagorinsky_cs > 0.0);
+  q.dfloor = d->dfloor;
+  q.cs = d->cs;
+  return cuda_check(launch_force_kick(d->dtype, q, s), "force kick kernels");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* jx_last_error(void) { return g_error; }
+
+const char* jx_version(void) { return "jx 0.1.0 (sm_103a)"; }
+
+int32_t jx_num_stages(int32_t integrator) {
+  return integrator == JX_RK2 ? 2 : (integrator == JX_RK3 ? 3 : (integrator == JX_RK4 ? 4 : 0));
+}
+
+jx_status jx_check_desc(const jx_desc* d) { return check_desc(d); }
+
+jx_status jx_tile_info(const jx_desc* d, int32_t* tile_x, int32_t* tile_y, int64_t* smem_bytes) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  Tile t;
+  if ((st = resolve_tile(d, &t))) return st;
+  if (tile_x) *tile_x = t.tx;
+  if (tile_y) *tile_y = t.ty;
+  if (smem_bytes) *smem_bytes = (int64_t)t.smem;
+  return JX_OK;
+}
+
+jx_status jx_workspace_bytes(const jx_desc* d, size_t* bytes) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!bytes) return fail(JX_ERR_INVALID, "null output pointer");
+  Tile t;
+  if ((st = resolve_tile(d, &t))) return st;
+  *bytes = layout_for(d, t).total;
+  return JX_OK;
+}
+
+jx_status jx_recover(const jx_desc* d, const void* U, void* U_out, void* W, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!U) return fail(JX_ERR_INVALID, "null state pointer");
+  return cuda_check(launch_recover(d->dtype, U, U_out, W, (int64_t)d->ny * d->nx, d->nvar, d->dfloor,
+                                   (cudaStream_t)s),
+                    "recover kernel");
+}
+
+jx_status jx_timestep(const jx_desc* d, const void* W, double cfl, double prev_dt, double time,
+                      double tlim, double* dt_out, void* workspace, size_t workspace_bytes,
+                      jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!W || !dt_out) return fail(JX_ERR_INVALID, "null W or dt_out");
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  CflParams q = cfl_params(d, W, nullptr, w);
+  if ((st = cuda_check(launch_cfl(d->dtype, true, q, (cudaStream_t)s), "cfl kernel"))) return st;
+  return cuda_check(launch_timestep_finish(dt_params(d), w.cfl, w.header, prev_dt, time, tlim, cfl,
+                                           dt_out, (cudaStream_t)s),
+                    "timestep finisher");
+}
+
+jx_status jx_stage(const jx_desc* d, int32_t stage, const void* U_in, const void* V_in, void* U_out,
+                   void* V_out, const void* tau, int32_t force_follows, jx_clock* clock,
+                   const jx_trace* trace, void* workspace, size_t workspace_bytes, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  return do_stage(d, t, w, stage, U_in, V_in, U_out, V_out, tau, force_follows, clock, trace,
+                  (cudaStream_t)s);
+}
+
+jx_status jx_cfl_partials(const jx_desc* d, const void* U, void* workspace, size_t workspace_bytes,
+                          jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!U) return fail(JX_ERR_INVALID, "null state pointer");
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  CflParams q = cfl_params(d, U, nullptr, w);
+  return cuda_check(launch_cfl(d->dtype, false, q, (cudaStream_t)s), "cfl kernel");
+}
+
+jx_status jx_begin_step(const jx_desc* d, jx_clock* clock, int32_t forced, void* workspace,
+                        size_t workspace_bytes, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!clock) return fail(JX_ERR_INVALID, "null clock");
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  return cuda_check(launch_begin_step(dt_params(d), clock, w.cfl, w.header, forced, (cudaStream_t)s),
+                    "begin-step kernel");
+}
+
+jx_status jx_force_render(const jx_desc* d, const jx_forcing* f, jx_clock* clock, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!f || !clock || !f->table || !f->cos_x || !f->sin_x || !f->cos_y || !f->sin_y || !f->raw_force)
+    return fail(JX_ERR_INVALID, "incomplete forcing tables");
+  if (f->n_modes < 1 || f->n_updates < 1) return fail(JX_ERR_INVALID, "forcing needs modes and updates");
+  RenderParams q;
+  q.clock = clock;
+  q.table = f->table;
+  q.cos_x = f->cos_x;
+  q.sin_x = f->sin_x;
+  q.cos_y = f->cos_y;
+  q.sin_y = f->sin_y;
+  q.raw = f->raw_force;
+  q.ny = d->ny;
+  q.nx = d->nx;
+  q.n_modes = f->n_modes;
+  q.n_updates = f->n_updates;
+  return cuda_check(launch_render(d->dtype, q, (cudaStream_t)s), "render kernel");
+}
+
+jx_status jx_force_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock,
+                        const jx_trace* trace, void* workspace, size_t workspace_bytes, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  return do_kick(d, f, U, clock, trace, w, (cudaStream_t)s);
+}
+
+jx_status jx_step(const jx_desc* d, void* S, void* A, void* B, const jx_forcing* forcing,
+                  jx_clock* clock, void* workspace, size_t workspace_bytes, jx_stream stream) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!S || !A || !B || !clock) return fail(JX_ERR_INVALID, "null state, scratch or clock pointer");
+  if (S == A || S == B || A == B) return fail(JX_ERR_INVALID, "S, A and B must be distinct buffers");
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int forced = forcing != nullptr;
+  if ((st = cuda_check(launch_begin_step(dt_params(d), clock, w.cfl, w.header, forced, s), "begin-step kernel")))
+    return st;
+  if (forced && (st = jx_force_render(d, forcing, clock, stream))) return st;
+  const int n = jx_num_stages(d->integrator);
+  // S -> A -> B -> A ... -> S; the saved register stays in S (pointwise).
+  const void* in = S;
+  for (int stage = 1; stage <= n; ++stage) {
+    void* out = stage == n ? S : (stage % 2 == 1 ? A : B);
+    if ((st = do_stage(d, t, w, stage, in, S, out, stage == n ? nullptr : S, nullptr, forced, clock,
+                       nullptr, s)))
+      return st;
+    in = out;
+  }
+  if (forced && (st = do_kick(d, forcing, S, clock, nullptr, w, s))) return st;
+  if (d->smagorinsky_cs > 0.0) {
+    CflParams q = cfl_params(d, S, clock, w);
+    if ((st = cuda_check(launch_cfl(d->dtype, false, q, s), "cfl kernel"))) return st;
+  }
+  return JX_OK;
+}
+
+jx_status jx_rk_stage(int32_t dtype, int64_t n, const void* U, const void* V, const void* div, double dt,
+                      double gam0, double gam1, double beta, double delta, int32_t has_delta,
+                      void* U_out, void* V_out, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (n < 0 || (n > 0 && (!U || !V || !div || !U_out))) return fail(JX_ERR_INVALID, "bad rk_stage arguments");
+  const int blend = gam0 != 0.0 && gam0 + gam1 == 1.0;
+  return cuda_check(launch_rk_stage(dtype, n, U, V, div, U_out, V_out, dt, gam0, gam1, beta, delta, has_delta,
+                                    blend, (cudaStream_t)s),
+                    "rk_stage kernel");
+}
+
+jx_status jx_flux_divergence(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, const void* flux_x,
+                             const void* flux_y, double dx, double dy, void* div, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (ny < 0 || nx < 0 || nv < 1) return fail(JX_ERR_INVALID, "bad shape");
+  if ((int64_t)ny * nx * nv > 0 && (!flux_x || !flux_y || !div)) return fail(JX_ERR_INVALID, "null array");
+  return cuda_check(launch_divergence(dtype, ny, nx, nv, flux_x, flux_y, 1.0 / dx, 1.0 / dy, div, (cudaStream_t)s),
+                    "divergence kernel");
+}
+
+jx_status jx_stress_face_fluxes(int32_t dtype, int32_t ny, int32_t nx, const void* tau, void* flux_x,
+                                void* flux_y, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (ny < 0 || nx < 0) return fail(JX_ERR_INVALID, "bad shape");
+  if ((int64_t)ny * nx > 0 && (!tau || !flux_x || !flux_y)) return fail(JX_ERR_INVALID, "null array");
+  return cuda_check(launch_stress_faces(dtype, ny, nx, tau, flux_x, flux_y, (cudaStream_t)s), "stress kernel");
+}
+
+jx_status jx_box_sums(const jx_desc* d, const void* U, double* out, void* workspace, size_t workspace_bytes,
+                      jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!U || !out) return fail(JX_ERR_INVALID, "null pointer");
+  Tile t;
+  Ws w;
+  if ((st = resolve_tile(d, &t)) || (st = bind_ws(d, t, workspace, workspace_bytes, &w))) return st;
+  return cuda_check(launch_box_sums(d->dtype, U, (int64_t)d->ny * d->nx, d->nvar, w.box, out, (cudaStream_t)s),
+                    "box-sum kernels");
+}
+
+jx_status jx_face_states(int32_t dtype, int32_t recon, int32_t ny, int32_t nx, int32_t nv, const void* W,
+                         int32_t axis, double dfloor, void* left, void* right, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (recon < JX_DC || recon > JX_WENOZ) return fail(JX_ERR_UNSUPPORTED, "unknown reconstruction %d", recon);
+  if (axis != 0 && axis != 1) return fail(JX_ERR_INVALID, "axis must be 0 (y) or 1 (x)");
+  if (ny < 0 || nx < 0 || nv < 1) return fail(JX_ERR_INVALID, "bad shape");
+  if ((int64_t)ny * nx * nv > 0 && (!W || !left || !right)) return fail(JX_ERR_INVALID, "null array");
+  static const FaceStatesLauncher table[5] = {face_states_dc, face_states_plm, face_states_ppm4, face_states_ppmx,
+                                              face_states_wenoz};
+  return cuda_check(table[recon](dtype, W, ny, nx, nv, axis, dfloor, left, right, (cudaStream_t)s),
+                    "face-state kernel");
+}
+
+jx_status jx_face_flux(int32_t dtype, int32_t rsolver, int64_t nface, int32_t nv, int32_t axis, const void* left,
+                       const void* right, double cs, void* flux, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (rsolver < JX_LLF || rsolver > JX_ROE) return fail(JX_ERR_UNSUPPORTED, "unknown Riemann solver %d", rsolver);
+  if (axis != 0 && axis != 1) return fail(JX_ERR_INVALID, "axis must be 0 (y) or 1 (x)");
+  if (nface < 0 || nv < 3) return fail(JX_ERR_INVALID, "bad shape");
+  if (nface > 0 && (!left || !right || !flux)) return fail(JX_ERR_INVALID, "null array");
+  return cuda_check(launch_face_flux(dtype, rsolver, nface, nv, axis, left, right, cs, flux, (cudaStream_t)s),
+                    "face-flux kernel");
+}
+
+jx_status jx_viscous_flux(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, const void* W, double dx, double dy,
+                          double viscosity, double smagorinsky_cs, int32_t axis, void* out, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (axis != 0 && axis != 1) return fail(JX_ERR_INVALID, "axis must be 0 (y) or 1 (x)");
+  if (ny < 0 || nx < 0 || nv < 3) return fail(JX_ERR_INVALID, "bad shape");
+  if ((int64_t)ny * nx > 0 && (!W || !out)) return fail(JX_ERR_INVALID, "null array");
+  return cuda_check(launch_viscous_flux(dtype, ny, nx, nv, W, dx, dy, viscosity, smagorinsky_cs, axis, out,
+                                        (cudaStream_t)s),
+                    "viscous-flux kernel");
+}
+
+jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sink, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (blocks < 1 || iters < 1 || !sink) return fail(JX_ERR_INVALID, "bad probe arguments");
+  return cuda_check(launch_probe(dtype, blocks, iters, sink, (cudaStream_t)s), "probe kernel");
+}
+
+}  // extern "C"

@@ -1,0 +1,15 @@
+// Stage-kernel instantiations for the wenoz reconstruction (float64 and
+// float32, all three Riemann solvers). One file per reconstruction keeps
+// the per-file compile short and lets the build run them in parallel.
+#include "jx_stage.cuh"
+
+namespace jx {
+cudaError_t launch_stage_wenoz(int dtype, int rsolver, const StageParams& p, dim3 grid, size_t smem,
+                            cudaStream_t s) {
+  return launch_stage_recon<JX_WENOZ>(dtype, rsolver, p, grid, smem, s);
+}
+cudaError_t face_states_wenoz(int dtype, const void* W, int ny, int nx, int nv, int axis, double dfloor,
+                           void* left, void* right, cudaStream_t s) {
+  return launch_face_states_recon<JX_WENOZ>(dtype, W, ny, nx, nv, axis, dfloor, left, right, s);
+}
+}  // namespace jx

@@ -1,0 +1,162 @@
+"""A device-resident solve: state, scratch, workspace, clock and forcing tables.
+
+One :class:`Solve` is one ``evolve_isothermal`` run (run.py:20-69). Its
+state lives in HBM for the whole run; every cycle is enqueued as one
+``jx_step`` (begin-step/dt, optional render, the fused stages, optional kick)
+and the host only reads the 128-byte clock back every ``steps_per_sync``
+cycles to learn whether tlim or nlim was reached. Runs without an SGS hook
+replay a CUDA graph of ``steps_per_sync`` captured cycles.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .hydro import RK_STAGES, _Forcing, make_desc, run_stages
+
+
+class Solve:
+    """Device-resident evolve_isothermal run."""
+
+    def __init__(self, U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *,
+                 viscosity=0.0, smagorinsky_cs=0.0, drag_rate=0.0, forcing=None,
+                 dt_update=1.0, tdriv_start=0.0, dedt=0.0, reconstruct="ppm4", rsolver="roe",
+                 predict_stress=None, sgs_weights=None, tile=(0, 0), dtype=None):
+        t = _lib.torch()
+        RK_STAGES[integrator]
+        self.U = _lib.to_device(U, dtype)
+        self.desc = make_desc(self.U.shape, self.U.dtype, dx, dy, cs, dfloor, integrator,
+                              viscosity=viscosity, smagorinsky_cs=smagorinsky_cs,
+                              drag_rate=drag_rate, reconstruct=reconstruct, rsolver=rsolver,
+                              tile=tile)
+        self.S = self.U.clone()
+        self.A = t.empty_like(self.S)
+        self.B = t.empty_like(self.S)
+        self.ws, self.nbytes = _lib.workspace(self.desc)
+        self.predict_stress, self.sgs_weights = predict_stress, sgs_weights
+        self.forcing = None
+        n_updates = 0
+        if forcing is not None:
+            from .forcing import _device_tables
+            coefficients, basis = forcing
+            tables = _device_tables(coefficients, basis, self.S.dtype)
+            if tables[1].shape[1] != self.S.shape[1] or tables[3].shape[1] != self.S.shape[0]:
+                raise ValueError("forcing basis does not match the grid")
+            raw = t.zeros(tuple(self.S.shape[:2]) + (2,), dtype=self.S.dtype, device=self.S.device)
+            self.forcing = _Forcing(raw, tables)
+            n_updates = tables[0].shape[0]
+        self.clock = _lib.new_clock(
+            tlim=float(tlim), nlim=int(nlim), cfl=float(cfl), t_start=float(tdriv_start),
+            dt_update=float(dt_update), dedt=float(dedt), n_updates=n_updates)
+        self._idle_clock = _lib.new_clock(done=1)
+        self.graph = None
+        self.graph_steps = 0
+        _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.ws),
+                  self.nbytes, _lib.stream_handle())
+
+    # -- enqueueing -----------------------------------------------------------
+    def enqueue_step(self, clock=None):
+        """Enqueue one full cycle (no SGS hook) on the current stream."""
+        clock = self.clock if clock is None else clock
+        forcing = ctypes.byref(self.forcing.struct) if self.forcing is not None else None
+        _lib.call("jx_step", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.A),
+                  _lib.ptr(self.B), forcing, _lib.ptr(clock), _lib.ptr(self.ws), self.nbytes,
+                  _lib.stream_handle())
+
+    def _hooked_step(self):
+        """One cycle with the SGS predictor: stages are driven from the host."""
+        stream = _lib.stream_handle()
+        forced = self.forcing is not None
+        _lib.call("jx_begin_step", ctypes.byref(self.desc), _lib.ptr(self.clock), int(forced),
+                  _lib.ptr(self.ws), self.nbytes, stream)
+        if _lib.read_clock(self.clock).done:
+            return False
+        if forced:
+            _lib.call("jx_force_render", ctypes.byref(self.desc), ctypes.byref(self.forcing.struct),
+                      _lib.ptr(self.clock), stream)
+        run_stages(self.desc, self.S, clock=self.clock, ws=self.ws, nbytes=self.nbytes,
+                   forcing=self.forcing, predict_stress=self.predict_stress,
+                   sgs_weights=self.sgs_weights, out=self.A)
+        self.S, self.A = self.A, self.S
+        if self.desc.smagorinsky_cs > 0.0:
+            _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S),
+                      _lib.ptr(self.ws), self.nbytes, stream)
+        return True
+
+    def capture(self, steps):
+        """Capture `steps` cycles into a CUDA graph (after a launch on an idle clock)."""
+        t = _lib.torch()
+        self.enqueue_step(self._idle_clock)  # sets per-kernel attributes; changes nothing
+        t.cuda.synchronize()
+        graph = t.cuda.CUDAGraph()
+        with t.cuda.graph(graph):
+            for _ in range(steps):
+                self.enqueue_step()
+        self.graph, self.graph_steps = graph, steps
+
+    # -- driving --------------------------------------------------------------
+    def state(self):
+        return _lib.read_clock(self.clock)
+
+    def run(self, steps_per_sync=32, use_graph=True):
+        """Advance until tlim or nlim; returns the final clock."""
+        if self.predict_stress is not None:
+            while self._hooked_step():
+                pass
+            return self.state()
+        if use_graph and self.graph is None:
+            self.capture(steps_per_sync)
+        while True:
+            if use_graph:
+                self.graph.replay()
+            else:
+                for _ in range(steps_per_sync):
+                    self.enqueue_step()
+            clock = self.state()
+            if clock.done:
+                return clock
+
+    def result(self):
+        c = self.state()
+        return self.S, c.time, c.prev_dt, c.cycle
+
+    def advance_host(self, U_host, out_host, steps=1):
+        """Load U from host memory, advance `steps` cycles, write the state back.
+
+        U_host/out_host are CPU tensors of the state's shape and dtype (pinned
+        memory makes both copies asynchronous). The CFL partials are
+        recomputed from the loaded state, as evolve_isothermal does at its
+        start. Nothing is synchronised here; the caller synchronises.
+        """
+        self.S.copy_(U_host, non_blocking=True)
+        _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.ws),
+                  self.nbytes, _lib.stream_handle())
+        for _ in range(steps):
+            self.enqueue_step()
+        out_host.copy_(self.S, non_blocking=True)
+
+    def enqueue_stage(self, stage, U_in, V_in, U_out, V_out=None):
+        """Enqueue one fused stage kernel alone (used to time the kernel in isolation)."""
+        _lib.call("jx_stage", ctypes.byref(self.desc), int(stage), _lib.ptr(U_in), _lib.ptr(V_in),
+                  _lib.ptr(U_out), _lib.ptr(V_out), None, 0, _lib.ptr(self.clock), None,
+                  _lib.ptr(self.ws), self.nbytes, _lib.stream_handle())
+
+    def set_clock(self, **fields):
+        """Overwrite clock fields from the host (synchronous, small)."""
+        c = self.state()
+        for key, value in fields.items():
+            setattr(c, key, value)
+        host = np.frombuffer(bytes(c), dtype=np.uint8).copy()
+        self.clock.copy_(_lib.torch().from_numpy(host))
+
+
+def check_evolve_args(viscosity, smagorinsky_cs, drag_rate, dedt, forcing, dt_update, tdriv_start):
+    """Argument checks of run.py:29-34."""
+    from math import isfinite
+    for name, value in (("viscosity", viscosity), ("smagorinsky_cs", smagorinsky_cs),
+                        ("drag_rate", drag_rate), ("dedt", dedt)):
+        if not isfinite(value) or value < 0.0:
+            raise ValueError(f"{name} must be finite and nonnegative")
+    if forcing is not None and (not 0.0 < dt_update < np.inf or not isfinite(tdriv_start)):
+        raise ValueError("dt_update must be finite and positive and tdriv_start finite")

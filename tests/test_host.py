@@ -1,0 +1,146 @@
+"""Host-side logic that needs no GPU: input decks, the OU table, RK schedule."""
+
+from itertools import islice
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from jathenax_gb300 import forcing as G
+from jathenax_gb300.hydro import RK_STAGES
+from jathenax_gb300.input import read_input
+from oracle import forcing_oracle as F
+from oracle import hydro_oracle as H
+
+DECK = """
+[problem]
+name = "turbulence"
+
+[mesh]
+nx = 256
+ny = 256
+
+[time]
+integrator = "rk3"
+cfl_number = 0.4
+tlim = 45.0
+nlim = 100000
+
+[hydro]
+iso_sound_speed = 1.0
+dfloor = 1.17549e-38
+reconstruct = "ppm4"
+rsolver = "roe"
+viscosity = 1.5e-6
+smagorinsky_cs = 0.0
+
+[hydro_srcterms]
+drag_rate = 0.3333335
+
+[turb_driving]
+rseed = 1618
+tcorr = 0.75
+dt_update = 0.0075
+tdriv_start = 0.0
+dedt = 0.03703705
+nlow = 3
+nhigh = 5
+npeak = 4
+sol_fraction = 1.0
+min_kx = -5
+max_kx = 5
+min_ky = -5
+max_ky = 5
+
+[output]
+file = "runs/driven_seed1618.npz"
+"""
+
+
+def test_seed1618_deck_equals_defaults(tmp_path):
+    path = tmp_path / "turbulence.toml"
+    path.write_text(DECK)
+    settings = read_input(path)
+    defaults = read_input(None, "turbulence")
+    defaults["output"]["file"] = "runs/driven_seed1618.npz"
+    assert settings == defaults
+
+
+@pytest.mark.parametrize(("contents", "message"), [
+    ("[hydro]\nviscosty = 0", "unknown input setting hydro.viscosty"),
+    ("[mesh]\nnx = true", "mesh.nx expects int"),
+    ("[turb_driving]\nrseed = 1", "unsupported input section"),
+    ("[problem]\nname = \"sod\"", "problem.name must be"),
+])
+def test_input_rejects_invalid_settings(tmp_path, contents, message):
+    path = tmp_path / "input.toml"
+    path.write_text(contents)
+    with pytest.raises(ValueError, match=message):
+        read_input(path)
+
+
+def test_rk_schedule_matches_oracle():
+    assert RK_STAGES == H.RK_TABLE
+    # Blend form exactly where the reference uses it (hydro.py:46).
+    forms = {k: [H.uses_blend_form(g0, g1) for g0, g1, _, _ in v] for k, v in RK_STAGES.items()}
+    assert forms == {"rk2": [False, True], "rk3": [False, True, True],
+                     "rk4": [False, False, False, False]}
+
+
+def test_host_random_streams_match_oracle_bitwise():
+    for seed in (0, 1, 1618, 2**31 - 5):
+        a = np.fromiter(islice(G.ran_st(seed), 500), float)
+        b = np.fromiter(islice(F.uniform_stream(seed), 500), float)
+        np.testing.assert_array_equal(a, b)
+        a = np.fromiter(islice(G.ran_gaussian_st(seed), 500), float)
+        b = np.fromiter(islice(F.gaussian_stream(seed), 500), float)
+        np.testing.assert_array_equal(a, b)
+
+
+def test_host_ou_table_matches_reference_fixture_bitwise(golden):
+    g = golden("forcing")
+    modes = G.cartesian_modes(3, 5, (-5, 5), (-5, 5))
+    np.testing.assert_array_equal(modes, g["modes"])
+    table = G.modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, 1618, 0.75, 0.0075, 7)
+    np.testing.assert_array_equal(table, g["table"])
+
+
+@pytest.mark.parametrize("kw", [dict(sol_fraction=0.3), dict(tcorr=0.0), dict(npeak=3.5)])
+def test_host_ou_table_variants_match_oracle(kw):
+    args = dict(nlow=2, nhigh=4, npeak=3.0, sol_fraction=1.0, rseed=7, tcorr=0.5, dt_update=0.01)
+    args.update(kw)
+    modes = G.cartesian_modes(args["nlow"], args["nhigh"], (-4, 4), (-4, 4))
+    a = G.modal_coefficients(modes, (1.0, 2.0), args["nlow"], args["nhigh"], args["npeak"],
+                             args["sol_fraction"], args["rseed"], args["tcorr"], args["dt_update"], 5)
+    b = F.ou_table(modes, (1.0, 2.0), args["nlow"], args["nhigh"], args["npeak"],
+                   args["sol_fraction"], args["rseed"], args["tcorr"], args["dt_update"], 5)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_forcing_argument_errors():
+    with pytest.raises(ValueError, match="1 <= nlow < nhigh"):
+        G.cartesian_modes(0, 3, (-3, 3), (-3, 3))
+    with pytest.raises(ValueError, match="no Cartesian forcing modes"):
+        G.cartesian_modes(8, 9, (-1, 1), (-1, 1))
+    modes = G.cartesian_modes(3, 5, (-5, 5), (-5, 5))
+    with pytest.raises(ValueError, match="npeak"):
+        G.modal_coefficients(modes, (1.0, 1.0), 3, 5, 6.0, 1.0, 1, 0.75, 0.0075, 2)
+    with pytest.raises(ValueError, match="tcorr"):
+        G.modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, 1, -1.0, 0.0075, 2)
+
+
+def test_evolve_argument_errors_before_any_device_work():
+    from jathenax_gb300.solver import check_evolve_args
+    with pytest.raises(ValueError, match="viscosity must be finite"):
+        check_evolve_args(-1.0, 0.0, 0.0, 0.0, None, 1.0, 0.0)
+    with pytest.raises(ValueError, match="dedt must be finite"):
+        check_evolve_args(0.0, 0.0, 0.0, float("inf"), None, 1.0, 0.0)
+    with pytest.raises(ValueError, match="dt_update"):
+        check_evolve_args(0.0, 0.0, 0.0, 0.0, object(), 0.0, 0.0)
+
+
+def test_no_oracle_import_in_package():
+    package = Path(__file__).resolve().parents[1] / "jathenax_gb300"
+    for path in package.rglob("*.py"):
+        text = path.read_text()
+        assert "import oracle" not in text and "from oracle" not in text, path
