@@ -50,6 +50,7 @@ def parse_args():
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
     p.add_argument("--n", type=int, default=4096, help="grid side (default 4096)")
     p.add_argument("--no-fp32", action="store_true", help="skip the float32 line")
+    p.add_argument("--only-fp32", action="store_true", help="time only the float32 state (profiling)")
     p.add_argument("--cpu-sample", type=int, default=512, help="grid side of the CPU sample")
     p.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU sample")
     return p.parse_args()
@@ -269,6 +270,10 @@ def bench_ours(args, world, rank, local):
     fp64_peak = fma_peak_tflops(torch, _lib, _lib.JX_F64)
     fp32_peak = fma_peak_tflops(torch, _lib, _lib.JX_F32)
 
+    if args.only_fp32:
+        r32 = run_precision(torch, _lib, Solve, U0, n, torch.float32, args, world)
+        return {"metric": METRIC, "value": round(r32["value"], 1), "unit": METRIC, "dtype": "f32",
+                "ms_per_step": round(r32["ms"] / args.steps, 4), "stage_ms": r32["stage_ms"]}
     r64 = run_precision(torch, _lib, Solve, U0, n, torch.float64, args, world,
                         clocks=nvidia_smi_index(local))
     r32 = None if args.no_fp32 else run_precision(torch, _lib, Solve, U0, n, torch.float32, args, world)
@@ -321,7 +326,7 @@ def bench_ours(args, world, rank, local):
                         "ms_per_step": round(r32["ms"] / args.steps, 4), "dtype": "f32",
                         "roofline": roofline(r32, 4, fp32_peak, "f32"), "e2e": r32["e2e"]}
         line["gpu_launches"] += 4 * args.steps
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
     return line
 

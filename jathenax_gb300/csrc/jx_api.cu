@@ -241,6 +241,8 @@ jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, cons
   p.visc_on = d->viscosity > 0.0 || d->smagorinsky_cs > 0.0;
   p.smag_on = d->smagorinsky_cs > 0.0;
   p.drag_on = d->drag_rate > 0.0;
+  fill_stage_consts(p.cd, p);
+  fill_stage_consts(p.cf, p);
   return cuda_check(launch_stage(d, p, t, s), "stage kernel");
 }
 

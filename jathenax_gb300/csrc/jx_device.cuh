@@ -1,10 +1,22 @@
-// Device-side building blocks of the fused isothermal stage kernel:
-// per-cell edge reconstructions, Riemann solvers, NaN-propagating min/max
-// and block reductions. Arithmetic follows the reference's operation order
-// (jathenax/fluxes.py), with two deliberate changes that the FP64 parity
-// tolerance (1e-12 relative per stage) covers: divisions by loop-invariant
-// constants (12, 6, cs, dx, dy) become multiplications by the reciprocal,
-// and nvcc contracts a*b+c into FMA.
+// Device-side building blocks of the fused isothermal stage kernel: exact
+// comparison/min/max primitives, the reconstructions split into a per-face
+// and a per-cell part, Riemann solvers, and block reductions.
+//
+// Arithmetic follows the reference's operation order (jathenax/fluxes.py)
+// with two deliberate changes that the float64 parity tolerance (1e-12
+// relative per stage) covers: divisions by loop-invariant constants (12, 6,
+// cs, dx, dy) become multiplications by the reciprocal, and nvcc contracts
+// a*b+c into FMA.
+//
+// GB300 executes float64 at 2 FMA per SM per clock, 1/64 of float32, while
+// the integer ALU is nearly idle in this kernel. For double precision the
+// comparisons, sign tests, min/max and absolute-value tests therefore run on
+// the IEEE bit patterns in the integer pipe. For every non-NaN operand they
+// select exactly what the floating-point comparison selects (the only
+// exception: a product a*b that underflows to +-0 is classified by the signs
+// of a and b); NaN operands are treated as large numbers instead of being
+// skipped by fmin/fmax, which only matters for a state that has already
+// failed. Single precision uses the native instructions.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -16,8 +28,7 @@ template <typename R> struct Tiny;
 template <> struct Tiny<double> { static constexpr double value = 2.2250738585072014e-308; };
 template <> struct Tiny<float> { static constexpr float value = 1.17549435e-38f; };
 
-// max/min that return NaN when either argument is NaN (jnp.maximum/minimum,
-// and jnp.max/min reductions), unlike fmax/fmin.
+// NaN-propagating max/min (jnp.maximum/minimum and the max/min reductions).
 template <typename T> __device__ __forceinline__ T nan_max(T a, T b) {
   return (a > b || a != a) ? a : b;
 }
@@ -26,135 +37,245 @@ template <typename T> __device__ __forceinline__ T nan_min(T a, T b) {
 }
 
 // ---------------------------------------------------------------------------
-// Reconstructions: (m2, m1, c, p1, p2) are one primitive at cells i-2..i+2;
-// produce the limited values at the low (lo) and high (hi) edges of cell i.
-// The face between cells i-1 and i takes left = hi(i-1), right = lo(i).
+// Exact comparison primitives. Num<R>::f(...) has the semantics of the
+// expression in its comment for non-NaN arguments.
 // ---------------------------------------------------------------------------
+template <typename R> struct Num;
 
+template <> struct Num<float> {
+  static __device__ __forceinline__ bool gt0(float x) { return x > 0.f; }          // x > 0
+  static __device__ __forceinline__ bool lt0(float x) { return x < 0.f; }          // x < 0
+  static __device__ __forceinline__ bool ge0(float x) { return x >= 0.f; }         // x >= 0
+  static __device__ __forceinline__ bool le0(float x) { return x <= 0.f; }         // x <= 0
+  static __device__ __forceinline__ float min(float a, float b) { return fminf(a, b); }
+  static __device__ __forceinline__ float max(float a, float b) { return fmaxf(a, b); }
+  // a, b >= 0 (no -0 ambiguity matters)
+  static __device__ __forceinline__ float pmin(float a, float b) { return fminf(a, b); }
+  static __device__ __forceinline__ float pmax(float a, float b) { return fmaxf(a, b); }
+  static __device__ __forceinline__ bool pge(float a, float b) { return a >= b; }  // a, b >= 0
+  static __device__ __forceinline__ bool pgt(float a, float b) { return a > b; }   // a, b >= 0
+  static __device__ __forceinline__ bool prod_ge0(float a, float b) { return a * b >= 0.f; }
+  static __device__ __forceinline__ bool prod_gt0(float a, float b) { return a * b > 0.f; }
+  static __device__ __forceinline__ bool prod_le0(float a, float b) { return a * b <= 0.f; }
+  // |a| >= 2|b|
+  static __device__ __forceinline__ bool abs_ge_twice(float a, float b) { return fabsf(a) >= 2.f * fabsf(b); }
+  static __device__ __forceinline__ bool lt(float a, float b) { return a < b; }    // a < b
+  // max of a >= 0 and b >= 0 or NaN, propagating NaN
+  static __device__ __forceinline__ float nanmax_pos(float a, float b) { return (b > a || b != b) ? b : a; }
+};
+
+template <> struct Num<double> {
+  static __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+  static constexpr long long kSign = (long long)0x8000000000000000ULL;
+  static constexpr long long kMag = 0x7fffffffffffffffLL;
+  // Monotone integer key: a < b  <=>  key(a) < key(b); -0 sorts just below +0.
+  static __device__ __forceinline__ long long key(double x) {
+    long long b = bits(x);
+    return b >= 0 ? b : (b ^ kMag);
+  }
+  static __device__ __forceinline__ bool zero(long long b) { return (b << 1) == 0; }
+  static __device__ __forceinline__ bool gt0(double x) { return bits(x) > 0; }
+  static __device__ __forceinline__ bool le0(double x) { return bits(x) <= 0; }
+  static __device__ __forceinline__ bool lt0(double x) { long long b = bits(x); return b < 0 && b != kSign; }
+  static __device__ __forceinline__ bool ge0(double x) { long long b = bits(x); return b >= 0 || b == kSign; }
+  static __device__ __forceinline__ double min(double a, double b) { return key(a) <= key(b) ? a : b; }
+  static __device__ __forceinline__ double max(double a, double b) { return key(a) >= key(b) ? a : b; }
+  static __device__ __forceinline__ double pmin(double a, double b) { return bits(a) <= bits(b) ? a : b; }
+  static __device__ __forceinline__ double pmax(double a, double b) { return bits(a) >= bits(b) ? a : b; }
+  static __device__ __forceinline__ bool pge(double a, double b) { return bits(a) >= bits(b); }
+  static __device__ __forceinline__ bool pgt(double a, double b) { return bits(a) > bits(b); }
+  static __device__ __forceinline__ bool prod_ge0(double a, double b) {
+    long long x = bits(a), y = bits(b);
+    return (x ^ y) >= 0 || zero(x) || zero(y);
+  }
+  static __device__ __forceinline__ bool prod_gt0(double a, double b) {
+    long long x = bits(a), y = bits(b);
+    return (x ^ y) >= 0 && !zero(x) && !zero(y);
+  }
+  static __device__ __forceinline__ bool prod_le0(double a, double b) { return !prod_gt0(a, b); }
+  static __device__ __forceinline__ bool abs_ge_twice(double a, double b) {
+    // Doubling |b| adds one to the exponent field of a normal number and
+    // doubles the bit pattern of a subnormal one.
+    const long long ua = bits(a) & kMag, ub = bits(b) & kMag;
+    const long long ub2 = ub < (1LL << 52) ? (ub << 1) : ub + (1LL << 52);
+    return ua >= ub2;
+  }
+  static __device__ __forceinline__ bool lt(double a, double b) { return key(a) < key(b); }
+  // max of a >= 0 and b >= 0 or NaN, propagating NaN (NaN of either sign
+  // compares above +inf once the sign bit is cleared)
+  static __device__ __forceinline__ double nanmax_pos(double a, double b) {
+    const long long x = bits(a) & kMag, y = bits(b) & kMag;
+    return y > x ? __longlong_as_double(y) : __longlong_as_double(x);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Reconstructions (fluxes.py:6-131). PPM4 and PPMX are split into the value
+// at a face, which both neighbouring cells share, and a per-cell limiter
+// that takes the cell's low/high face values; DC, PLM and WENO-Z produce the
+// cell's low/high edges directly from its stencil.
+// ---------------------------------------------------------------------------
+template <int RECON> struct ReconTraits {
+  static constexpr bool kFaceShared = RECON == 2 || RECON == 3;  // ppm4, ppmx
+  static constexpr int kHalo = RECON == 0 ? 1 : (RECON == 1 ? 2 : 3);
+};
+
+// Fourth-order interpolant at the face between w1 and w2 (fluxes.py:29-30).
 template <typename R>
-__device__ __forceinline__ void edges_dc(R, R, R c, R, R, R& lo, R& hi) {
-  lo = c;  // fluxes.py:6-8
-  hi = c;
+__device__ __forceinline__ R ppm_interp(R w0, R w1, R w2, R w3) {
+  return (R(7) * (w2 + w1) - (w0 + w3)) * R(1.0 / 12.0);
 }
 
+// PPM4 face value: interpolant bounded by the two neighbours (fluxes.py:29-32).
 template <typename R>
-__device__ __forceinline__ void edges_plm(R, R m1, R c, R p1, R, R& lo, R& hi) {
-  // fluxes.py:11-18, harmonic-mean slope.
-  R bw = c - m1;
-  R fw = p1 - c;
-  R prod = bw * fw;
-  R hs = prod > R(0) ? prod / (bw + fw) : R(0);
-  hi = c + hs;
-  lo = c - hs;
+__device__ __forceinline__ R ppm4_face(R w0, R w1, R w2, R w3) {
+  using N = Num<R>;
+  const R e = ppm_interp(w0, w1, w2, w3);
+  return N::min(N::max(e, N::min(w2, w1)), N::max(w2, w1));
 }
 
+// PPM4 cell limiter (fluxes.py:35-42).
 template <typename R>
-__device__ __forceinline__ void edges_ppm4(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
-  // fluxes.py:21-42.
-  const R k12 = R(1.0 / 12.0);
-  R l = (R(7) * (c + m1) - (m2 + p1)) * k12;
-  R h = (R(7) * (c + p1) - (m1 + p2)) * k12;
-  l = fmin(fmax(l, fmin(c, m1)), fmax(c, m1));
-  h = fmin(fmax(h, fmin(c, p1)), fmax(c, p1));
-  R dh = h - c;
-  R dl = l - c;
-  bool flat = dh * dl >= R(0);
-  R l2 = fabs(dl) >= R(2) * fabs(dh) ? c - R(2) * dh : l;
-  R h2 = fabs(dh) >= R(2) * fabs(dl) ? c - R(2) * dl : h;
+__device__ __forceinline__ void ppm4_cell(R c, R lo_face, R hi_face, R& lo, R& hi) {
+  using N = Num<R>;
+  const R dh = hi_face - c;
+  const R dl = lo_face - c;
+  const bool flat = N::prod_ge0(dh, dl);
+  const R l2 = N::abs_ge_twice(dl, dh) ? c - R(2) * dh : lo_face;
+  const R h2 = N::abs_ge_twice(dh, dl) ? c - R(2) * dl : hi_face;
   lo = flat ? c : l2;
   hi = flat ? c : h2;
 }
 
+// Smooth-extremum limiter of one face value (fluxes.py:45-53).
 template <typename R>
 __device__ __forceinline__ R ppmx_edge(R a, R b, R edge, R ca, R cb) {
-  // fluxes.py:45-53.
-  R curv = R(3) * ((a + b) - R(2) * edge);
-  bool agree = (curv > R(0) && ca > R(0) && cb > R(0)) || (curv < R(0) && ca < R(0) && cb < R(0));
-  R mag = fmin(fabs(ca), fabs(cb));
-  R lim = copysign(fmin(R(1.25) * mag, fabs(curv)), curv);
-  R fixed = R(0.5) * (a + b) - (agree ? lim : R(0)) * R(1.0 / 6.0);
-  return (a - edge) * (b - edge) > R(0) ? fixed : edge;
+  using N = Num<R>;
+  const R curv = R(3) * ((a + b) - R(2) * edge);
+  const bool agree = (N::gt0(curv) && N::gt0(ca) && N::gt0(cb)) || (N::lt0(curv) && N::lt0(ca) && N::lt0(cb));
+  const R mag = N::pmin(fabs(ca), fabs(cb));
+  const R lim = copysign(N::pmin(R(1.25) * mag, fabs(curv)), curv);
+  const R fixed = R(0.5) * (a + b) - (agree ? lim : R(0)) * R(1.0 / 6.0);
+  return N::prod_gt0(a - edge, b - edge) ? fixed : edge;
 }
 
+// PPMX face value between w1 and w2 (fluxes.py:62-68).
 template <typename R>
-__device__ __forceinline__ void edges_ppmx(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
-  // fluxes.py:56-84.
-  const R k12 = R(1.0 / 12.0);
-  R l = (R(7) * (c + m1) - (m2 + p1)) * k12;
-  R h = (R(7) * (c + p1) - (m1 + p2)) * k12;
-  R cl = (m2 + c) - R(2) * m1;
-  R cm = (m1 + p1) - R(2) * c;
-  R cr = (c + p2) - R(2) * p1;
-  l = ppmx_edge(m1, c, l, cl, cm);
-  h = ppmx_edge(c, p1, h, cm, cr);
-  R dh = h - c;
-  R dl = l - c;
-  bool ext = (dh * (c - l) <= R(0)) || ((m1 - c) * (c - p1) <= R(0));
-  R d2 = R(6) * ((l + h) - R(2) * c);
-  bool agree = (d2 > R(0) && cl > R(0) && cm > R(0) && cr > R(0)) ||
-               (d2 < R(0) && cl < R(0) && cm < R(0) && cr < R(0));
-  R mag = fmin(fabs(cm), fmin(fabs(cl), fabs(cr)));
-  R lim = copysign(fmin(R(1.25) * mag, fabs(d2)), d2);
-  R scale = fmax(fabs(m1), fmax(fabs(c), fabs(p1)));
-  bool use = agree && (fabs(d2) > R(1e-12) * scale);
-  R ratio = use ? lim / d2 : R(0);
-  R lm = fabs(dl) >= R(2) * fabs(dh) ? c - R(2) * dh : l;
-  R hm = fabs(dh) >= R(2) * fabs(dl) ? c - R(2) * dl : h;
+__device__ __forceinline__ R ppmx_face(R w0, R w1, R w2, R w3) {
+  const R e = ppm_interp(w0, w1, w2, w3);
+  const R c1 = (w0 + w2) - R(2) * w1;
+  const R c2 = (w1 + w3) - R(2) * w2;
+  return ppmx_edge(w1, w2, e, c1, c2);
+}
+
+// PPMX cell limiter (fluxes.py:70-84).
+template <typename R>
+__device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face, R hi_face, R& lo, R& hi) {
+  using N = Num<R>;
+  const R cl = (m2 + c) - R(2) * m1;
+  const R cm = (m1 + p1) - R(2) * c;
+  const R cr = (c + p2) - R(2) * p1;
+  const R dh = hi_face - c;
+  const R dl = lo_face - c;
+  const bool ext = N::prod_le0(dh, c - lo_face) || N::prod_le0(m1 - c, c - p1);
+  const R d2 = R(6) * ((lo_face + hi_face) - R(2) * c);
+  const bool agree = (N::gt0(d2) && N::gt0(cl) && N::gt0(cm) && N::gt0(cr)) ||
+                     (N::lt0(d2) && N::lt0(cl) && N::lt0(cm) && N::lt0(cr));
+  const R mag = N::pmin(fabs(cm), N::pmin(fabs(cl), fabs(cr)));
+  const R lim = copysign(N::pmin(R(1.25) * mag, fabs(d2)), d2);
+  const R scale = N::pmax(fabs(m1), N::pmax(fabs(c), fabs(p1)));
+  const bool use = agree && N::pgt(fabs(d2), R(1e-12) * scale);
+  R ratio = R(0);
+  if (use) ratio = lim / d2;
+  const R lm = N::abs_ge_twice(dl, dh) ? c - R(2) * dh : lo_face;
+  const R hm = N::abs_ge_twice(dh, dl) ? c - R(2) * dl : hi_face;
   lo = ext ? c + dl * ratio : lm;
   hi = ext ? c + dh * ratio : hm;
 }
 
 template <typename R>
+__device__ __forceinline__ void plm_cell(R m1, R c, R p1, R& lo, R& hi) {
+  // fluxes.py:11-18, harmonic-mean slope.
+  using N = Num<R>;
+  const R bw = c - m1;
+  const R fw = p1 - c;
+  R hs = R(0);
+  if (N::prod_gt0(bw, fw)) hs = (bw * fw) / (bw + fw);
+  hi = c + hs;
+  lo = c - hs;
+}
+
+template <typename R>
 __device__ __forceinline__ R wenoz_combine(R s0, R s1, R s2, R s3, R s4, R w0, R w1, R w2) {
   // fluxes.py:87-93.
-  R a0 = R(0.1) * w0, a1 = R(0.6) * w1, a2 = R(0.3) * w2;
-  R f0 = R(2) * s0 - R(7) * s1 + R(11) * s2;
-  R f1 = -s1 + R(5) * s2 + R(2) * s3;
-  R f2 = R(2) * s2 + R(5) * s3 - s4;
+  const R a0 = R(0.1) * w0, a1 = R(0.6) * w1, a2 = R(0.3) * w2;
+  const R f0 = R(2) * s0 - R(7) * s1 + R(11) * s2;
+  const R f1 = -s1 + R(5) * s2 + R(2) * s3;
+  const R f2 = R(2) * s2 + R(5) * s3 - s4;
   return (f0 * a0 + f1 * a1 + f2 * a2) / (R(6) * (a0 + a1 + a2));
 }
 
 template <typename R>
-__device__ __forceinline__ void edges_wenoz(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
+__device__ __forceinline__ void wenoz_cell(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
   // fluxes.py:96-117; eps = max(1e-42, finfo(dtype).tiny) at fluxes.py:108.
+  using N = Num<R>;
   const R k1312 = R(13.0 / 12.0);
   const R eps = R(1e-42) > Tiny<R>::value ? R(1e-42) : Tiny<R>::value;
-  R t0 = (m2 + c) - R(2) * m1, u0 = (m2 + R(3) * c) - R(4) * m1;
-  R t1 = (m1 + p1) - R(2) * c, u1 = m1 - p1;
-  R t2 = (p2 + c) - R(2) * p1, u2 = (p2 + R(3) * c) - R(4) * p1;
-  R b0 = k1312 * (t0 * t0) + R(0.25) * (u0 * u0);
-  R b1 = k1312 * (t1 * t1) + R(0.25) * (u1 * u1);
-  R b2 = k1312 * (t2 * t2) + R(0.25) * (u2 * u2);
-  R tau = fabs(b0 - b2);
-  R d0 = b0 + eps, d1 = b1 + eps, d2 = b2 + eps;
-  R dmin = fmin(d0, fmin(d1, d2));
-  R inv_sc = R(1) / fmax(tau, dmin);
+  const R t0 = (m2 + c) - R(2) * m1, u0 = (m2 + R(3) * c) - R(4) * m1;
+  const R t1 = (m1 + p1) - R(2) * c, u1 = m1 - p1;
+  const R t2 = (p2 + c) - R(2) * p1, u2 = (p2 + R(3) * c) - R(4) * p1;
+  const R b0 = k1312 * (t0 * t0) + R(0.25) * (u0 * u0);
+  const R b1 = k1312 * (t1 * t1) + R(0.25) * (u1 * u1);
+  const R b2 = k1312 * (t2 * t2) + R(0.25) * (u2 * u2);
+  const R tau = fabs(b0 - b2);
+  const R d0 = b0 + eps, d1 = b1 + eps, d2 = b2 + eps;
+  const R dmin = N::pmin(d0, N::pmin(d1, d2));
+  const R inv_sc = R(1) / N::pmax(tau, dmin);
   R base = dmin * inv_sc;
   base = base * base;
-  R con = tau * inv_sc;
-  R r0 = con * (dmin / d0), r1 = con * (dmin / d1), r2 = con * (dmin / d2);
-  R w0 = base + r0 * r0, w1 = base + r1 * r1, w2 = base + r2 * r2;
+  const R con = tau * inv_sc;
+  const R r0 = con * (dmin / d0), r1 = con * (dmin / d1), r2 = con * (dmin / d2);
+  const R w0 = base + r0 * r0, w1 = base + r1 * r1, w2 = base + r2 * r2;
   hi = wenoz_combine(m2, m1, c, p1, p2, w0, w1, w2);
   lo = wenoz_combine(p2, p1, c, m1, m2, w2, w1, w0);
 }
 
+// Face value shared by the two cells at a face (PPM4/PPMX only).
 template <int RECON, typename R>
-__device__ __forceinline__ void edges(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
-  if constexpr (RECON == 0) edges_dc(m2, m1, c, p1, p2, lo, hi);
-  else if constexpr (RECON == 1) edges_plm(m2, m1, c, p1, p2, lo, hi);
-  else if constexpr (RECON == 2) edges_ppm4(m2, m1, c, p1, p2, lo, hi);
-  else if constexpr (RECON == 3) edges_ppmx(m2, m1, c, p1, p2, lo, hi);
-  else edges_wenoz(m2, m1, c, p1, p2, lo, hi);
+__device__ __forceinline__ R face_value(R w0, R w1, R w2, R w3) {
+  if constexpr (RECON == 2) return ppm4_face(w0, w1, w2, w3);
+  else return ppmx_face(w0, w1, w2, w3);
 }
 
-// Ghost-cell depth a tile needs: the cells -1..n of a sweep use a stencil of
-// half-width 0 (dc), 1 (plm) or 2 (ppm4/ppmx/wenoz); viscous gradients need 1.
-template <int RECON> struct TileHalo { static constexpr int value = RECON == 0 ? 1 : (RECON == 1 ? 2 : 3); };
+// Low/high edges of the cell at the centre of (m2, m1, c, p1, p2); for the
+// face-shared methods lo_face/hi_face are the cell's two face values.
+template <int RECON, typename R>
+__device__ __forceinline__ void cell_edges(R m2, R m1, R c, R p1, R p2, R lo_face, R hi_face,
+                                           R& lo, R& hi) {
+  if constexpr (RECON == 0) { lo = c; hi = c; }
+  else if constexpr (RECON == 1) plm_cell(m1, c, p1, lo, hi);
+  else if constexpr (RECON == 2) ppm4_cell(c, lo_face, hi_face, lo, hi);
+  else if constexpr (RECON == 3) ppmx_cell(m2, m1, c, p1, p2, lo_face, hi_face, lo, hi);
+  else wenoz_cell(m2, m1, c, p1, p2, lo, hi);
+}
+
+// Both edges of a cell from its 5-point stencil (+1 more on each side for
+// the face-shared methods): used by the standalone face-state kernel.
+template <int RECON, typename R>
+__device__ __forceinline__ void edges_from_stencil(R m3, R m2, R m1, R c, R p1, R p2, R p3, R& lo, R& hi) {
+  R lf = R(0), hf = R(0);
+  if constexpr (ReconTraits<RECON>::kFaceShared) {
+    lf = face_value<RECON>(m2, m1, c, p1);
+    hf = face_value<RECON>(m1, c, p1, p2);
+  }
+  (void)m3;
+  (void)p3;
+  cell_edges<RECON>(m2, m1, c, p1, p2, lf, hf, lo, hi);
+}
 
 // ---------------------------------------------------------------------------
 // Riemann solvers in the (normal, tangential) frame (fluxes.py:134-201).
 // ---------------------------------------------------------------------------
-
 template <typename R> struct Gas {
   R cs, cs2, inv_cs, half_inv_cs;
 };
@@ -163,12 +284,13 @@ template <typename R>
 __device__ __forceinline__ void flux_llf(R dl, R dr, R ul, R ur, R tl, R tr, const Gas<R>& g,
                                          R& f0, R& f1, R& f2) {
   // fluxes.py:175-183.
-  R ml = dl * ul, mr = dr * ur;
-  R ql = dl * tl, qr = dr * tr;
-  R s0 = ml + mr;
-  R s1 = ml * ul + mr * ur + g.cs2 * (dl + dr);
-  R s2 = ml * tl + mr * tr;
-  R sp = fmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
+  using N = Num<R>;
+  const R ml = dl * ul, mr = dr * ur;
+  const R ql = dl * tl, qr = dr * tr;
+  const R s0 = ml + mr;
+  const R s1 = ml * ul + mr * ur + g.cs2 * (dl + dr);
+  const R s2 = ml * tl + mr * tr;
+  const R sp = N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
   f0 = R(0.5) * (s0 - sp * (dr - dl));
   f1 = R(0.5) * (s1 - sp * (mr - ml));
   f2 = R(0.5) * (s2 - sp * (qr - ql));
@@ -178,16 +300,17 @@ template <typename R>
 __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, const Gas<R>& g,
                                           R& f0, R& f1, R& f2) {
   // fluxes.py:186-201.
-  R sl = sqrt(dl), sr = sqrt(dr);
-  R u = (sl * ul + sr * ur) * (R(1) / (sl + sr));
-  R alo = fmin(u - g.cs, ul - g.cs);
-  R ahi = fmax(u + g.cs, ur + g.cs);
-  R bm = alo < R(0) ? alo : R(-1e-20);
-  R bp = ahi > R(0) ? ahi : R(1e-20);
-  R vl = ul - bm, vr = ur - bp;
-  R fl0 = dl * vl, fl1 = dl * ul * vl + g.cs2 * dl, fl2 = dl * tl * vl;
-  R fr0 = dr * vr, fr1 = dr * ur * vr + g.cs2 * dr, fr2 = dr * tr * vr;
-  R w = R(0.5) * (bp + bm) / (bp - bm);
+  using N = Num<R>;
+  const R sl = sqrt(dl), sr = sqrt(dr);
+  const R u = (sl * ul + sr * ur) * (R(1) / (sl + sr));
+  const R alo = N::min(u - g.cs, ul - g.cs);
+  const R ahi = N::max(u + g.cs, ur + g.cs);
+  const R bm = N::lt0(alo) ? alo : R(-1e-20);
+  const R bp = N::gt0(ahi) ? ahi : R(1e-20);
+  const R vl = ul - bm, vr = ur - bp;
+  const R fl0 = dl * vl, fl1 = dl * ul * vl + g.cs2 * dl, fl2 = dl * tl * vl;
+  const R fr0 = dr * vr, fr1 = dr * ur * vr + g.cs2 * dr, fr2 = dr * tr * vr;
+  const R w = R(0.5) * (bp + bm) / (bp - bm);
   f0 = R(0.5) * (fl0 + fr0) + w * (fl0 - fr0);
   f1 = R(0.5) * (fl1 + fr1) + w * (fl1 - fr1);
   f2 = R(0.5) * (fl2 + fr2) + w * (fl2 - fr2);
@@ -197,34 +320,34 @@ template <typename R>
 __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, const Gas<R>& g,
                                          R& f0, R& f1, R& f2) {
   // fluxes.py:134-172.
-  R ml = dl * ul, mr = dr * ur;
-  R ql = dl * tl, qr = dr * tr;
-  R pl = g.cs2 * dl, pr = g.cs2 * dr;
-  R l0 = ml, l1 = ml * ul + pl, l2 = ml * tl;
-  R r0 = mr, r1 = mr * ur + pr, r2 = mr * tr;
-  R a0 = R(0.5) * (l0 + r0), a1 = R(0.5) * (l1 + r1), a2 = R(0.5) * (l2 + r2);
-  R sl = sqrt(dl), sr = sqrt(dr);
-  R inv = R(1) / (sl + sr);
-  R u = (sl * ul + sr * ur) * inv;
-  R t = (sl * tl + sr * tr) * inv;
-  R lm = u - g.cs, lp = u + g.cs;
-  R jd = dr - dl, jm = mr - ml, jq = qr - ql;
-  R hu = (R(0.5) * u) * g.inv_cs;
-  R jmc = jm * g.half_inv_cs;
-  R am = jd * (R(0.5) + hu) - jmc;
-  R az = jd * (-t) + jq;
-  R ap = jd * (R(0.5) - hu) + jmc;
-  R km = R(-0.5) * fabs(lm) * am;
-  R kz = R(-0.5) * fabs(u) * az;
-  R kp = R(-0.5) * fabs(lp) * ap;
+  using N = Num<R>;
+  const R ml = dl * ul, mr = dr * ur;
+  const R ql = dl * tl, qr = dr * tr;
+  const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
+  const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
+  const R a0 = R(0.5) * (l0 + r0), a1 = R(0.5) * (l1 + r1), a2 = R(0.5) * (l2 + r2);
+  const R sl = sqrt(dl), sr = sqrt(dr);
+  const R inv = R(1) / (sl + sr);
+  const R u = (sl * ul + sr * ur) * inv;
+  const R t = (sl * tl + sr * tr) * inv;
+  const R lm = u - g.cs, lp = u + g.cs;
+  const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
+  const R hu = (R(0.5) * u) * g.inv_cs;
+  const R jmc = jm * g.half_inv_cs;
+  const R am = jd * (R(0.5) + hu) - jmc;
+  const R az = jd * (-t) + jq;
+  const R ap = jd * (R(0.5) - hu) + jmc;
+  const R km = R(-0.5) * fabs(lm) * am;
+  const R kz = R(-0.5) * fabs(u) * az;
+  const R kp = R(-0.5) * fabs(lp) * ap;
   R g0 = a0 + km + kp;
   R g1 = a1 + km * lm + kp * lp;
   R g2 = a2 + km * t + kz + kp * t;
-  if (lm >= R(0)) { g0 = l0; g1 = l1; g2 = l2; }
-  if (lp <= R(0)) { g0 = r0; g1 = r1; g2 = r2; }
-  R dstar = dl + am;
-  if (dstar < R(0) || dstar + ap < R(0)) {
-    R sp = R(0.5) * fmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
+  if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
+  if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
+  const R dstar = dl + am;
+  if (N::lt0(dstar) || N::lt0(dstar + ap)) {
+    const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
     g0 = a0 - sp * jd;
     g1 = a1 - sp * jm;
     g2 = a2 - sp * jq;
@@ -245,7 +368,6 @@ __device__ __forceinline__ void riemann(R dl, R dr, R ul, R ur, R tl, R tr, cons
 // ---------------------------------------------------------------------------
 // Reductions.
 // ---------------------------------------------------------------------------
-
 __device__ __forceinline__ double warp_nan_max(double v) {
   for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;

@@ -22,6 +22,15 @@ struct WsHeader {
   int64_t pad[31];
 };
 
+// Loop-invariant constants of one stage, precomputed on the host in the
+// state's precision (no per-thread float64 work in the float32 kernel).
+template <typename R> struct StageConsts {
+  R cs, cs2, inv_cs, half_inv_cs;
+  R inv_dx, inv_dy, inv_4dx, inv_4dy;
+  R dfloor, nu, smag_c, drag;
+  R g0, g1, delta;
+};
+
 struct StageParams {
   const void* U;      // stage input, read with halo
   const void* V;      // saved register, pointwise
@@ -36,8 +45,33 @@ struct StageParams {
   double dx, dy, inv_dx, inv_dy, inv_4dx, inv_4dy;
   double cs, dfloor, nu, smag_c, drag;
   double g0, g1, beta, delta;
+  StageConsts<double> cd;
+  StageConsts<float> cf;
   int has_delta, blend, floor_v, floor_out, want_cfl, visc_on, smag_on, drag_on, trace_on;
 };
+
+template <typename R> __host__ __device__ inline const StageConsts<R>& stage_consts(const StageParams& p);
+template <> __host__ __device__ inline const StageConsts<double>& stage_consts<double>(const StageParams& p) { return p.cd; }
+template <> __host__ __device__ inline const StageConsts<float>& stage_consts<float>(const StageParams& p) { return p.cf; }
+
+template <typename R>
+inline void fill_stage_consts(StageConsts<R>& c, const StageParams& p) {
+  c.cs = (R)p.cs;
+  c.cs2 = (R)(p.cs * p.cs);
+  c.inv_cs = (R)(1.0 / p.cs);
+  c.half_inv_cs = (R)(0.5 / p.cs);
+  c.inv_dx = (R)p.inv_dx;
+  c.inv_dy = (R)p.inv_dy;
+  c.inv_4dx = (R)p.inv_4dx;
+  c.inv_4dy = (R)p.inv_4dy;
+  c.dfloor = (R)p.dfloor;
+  c.nu = (R)p.nu;
+  c.smag_c = (R)p.smag_c;
+  c.drag = (R)p.drag;
+  c.g0 = (R)p.g0;
+  c.g1 = (R)p.g1;
+  c.delta = (R)p.delta;
+}
 
 // Launchers defined in stage_<recon>.cu.
 typedef cudaError_t (*StageLauncher)(int dtype, int rsolver, const StageParams& p, dim3 grid,
@@ -57,13 +91,30 @@ cudaError_t face_states_ppm4(int, const void*, int, int, int, int, double, void*
 cudaError_t face_states_ppmx(int, const void*, int, int, int, int, double, void*, void*, cudaStream_t);
 cudaError_t face_states_wenoz(int, const void*, int, int, int, int, double, void*, void*, cudaStream_t);
 
-// Shared-memory bytes of one stage tile.
+// Shared-memory planes of one stage tile, per variable: primitives with
+// halo, x fluxes, y fluxes, face values (PPM4/PPMX), right face states.
+struct TilePlanes {
+  int halo, pw, ph, w, fx, fy, a, r;
+  __host__ __device__ size_t per_var() const { return (size_t)w + fx + fy + a + r; }
+};
+
+__host__ __device__ inline TilePlanes tile_planes(int recon, int tx, int ty) {
+  TilePlanes t;
+  t.halo = recon == JX_DC ? 1 : (recon == JX_PLM ? 2 : 3);
+  t.pw = tx + 2 * t.halo;
+  t.ph = ty + 2 * t.halo;
+  t.w = t.pw * t.ph;
+  t.fx = ty * (tx + 1);
+  t.fy = (ty + 1) * tx;
+  const bool shared = recon == JX_PPM4 || recon == JX_PPMX;
+  const int ax = ty * (tx + 3), ay = (ty + 3) * tx;
+  t.a = shared ? (ax > ay ? ax : ay) : 0;
+  t.r = t.fx > t.fy ? t.fx : t.fy;
+  return t;
+}
+
 inline size_t stage_smem_bytes(int recon, int dtype, int nv, int tx, int ty) {
-  int h = recon == JX_DC ? 1 : (recon == JX_PLM ? 2 : 3);
-  size_t w = dtype == JX_F64 ? 8 : 4;
-  size_t cells = (size_t)nv * ((size_t)(tx + 2 * h) * (ty + 2 * h) +
-                               2 * (size_t)ty * (tx + 1) + 2 * (size_t)(ty + 1) * tx);
-  return cells * w;
+  return (size_t)nv * tile_planes(recon, tx, ty).per_var() * (dtype == JX_F64 ? 8 : 4);
 }
 
 }  // namespace jx

@@ -152,10 +152,10 @@ def main():
                 kh_dt=np.asarray(out[2]), kh_cycle=np.asarray(out[3]))
     U = np.zeros((ny, nx, 3))
     U[..., 0] = 1.0
-    updates = 4
+    updates = int(np.ceil(0.5 / 0.0075)) + 1
     table = forcing.modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, 1618, 0.75, 0.0075, updates)
     basis = forcing.forcing_basis(jnp.asarray(modes), jnp.asarray(x), jnp.asarray(x), (1.0, 1.0))
-    out = run.evolve_isothermal(jnp.asarray(U), 1 / nx, 1 / ny, 1.0, 1.17549e-38, "rk3", 0.4, 0.02, 12,
+    out = run.evolve_isothermal(jnp.asarray(U), 1 / nx, 1 / ny, 1.0, 1.17549e-38, "rk3", 0.4, 0.5, 12,
                                 viscosity=1.5e-6, drag_rate=0.3333335,
                                 forcing=(jnp.asarray(table), basis), dt_update=0.0075,
                                 tdriv_start=0.0, dedt=0.03703705)

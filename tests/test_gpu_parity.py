@@ -172,7 +172,7 @@ def test_forced_turbulence_run_matches_reference(golden):
     x = (np.arange(32) + 0.5) / 32 - 0.5
     basis = forcing_basis(cartesian_modes(3, 5, (-5, 5), (-5, 5)), x, x, (1.0, 1.0))
     U, time, _, cycle = evolve_isothermal(
-        g["turb_U0"], 1 / 32, 1 / 32, 1.0, 1.17549e-38, "rk3", 0.4, 0.02, 12, viscosity=1.5e-6,
+        g["turb_U0"], 1 / 32, 1 / 32, 1.0, 1.17549e-38, "rk3", 0.4, 0.5, 12, viscosity=1.5e-6,
         drag_rate=0.3333335, forcing=(g["turb_table"], basis), dt_update=0.0075, dedt=0.03703705)
     assert cycle == g["turb_cycle"] == 12
     assert_rel(time, g["turb_time"], RUN_RTOL)
@@ -255,3 +255,47 @@ def test_step_is_deterministic_and_conservative_at_1024(G):
     after = a.sum(dim=(0, 1))
     scale = U0.abs().sum(dim=(0, 1))
     assert torch.all((after - before).abs() <= 1e-13 * scale)
+
+
+def tie_heavy_state(nx, ny, nvar, kind):
+    """States full of exact ties, zeros and subnormal differences for the limiters.
+
+    Densities are powers of two so that v = m / rho is recovered exactly and
+    flat stencils stay exactly flat (otherwise rounding noise of 1e-17 sets
+    the WENO-Z weights, whose epsilon is 1e-42, and the comparison measures
+    noise amplification rather than the kernel).
+    """
+    x, y = R.cell_centers(nx, ny)
+    X, Y = np.meshgrid(x, y)
+    if kind == "steps":        # piecewise constant: flat stencils and jumps
+        rho = np.where(np.abs(Y) < 0.25, 2.0, 1.0) * np.where(X > 0.1, 0.5, 1.0)
+        vx = np.where(np.abs(Y) < 0.25, 0.5, -0.5)
+        vy = np.zeros_like(X)
+    elif kind == "linear":     # staircases: exact |dl| = |dh| ties
+        rho = 2.0 ** np.round(X * 4)
+        vx = 0.25 * np.round(Y * 16) / 16
+        vy = -vx
+    else:                      # subnormal-sized perturbations around exact values
+        rho = 1.0 + np.where((np.arange(nx)[None, :] + np.arange(ny)[:, None]) % 3 == 0, 1e-300, 0.0)
+        vx = np.where(X > 0, 5e-310, -5e-310) + 0.0 * Y
+        vy = np.where(Y > 0, 0.0, -0.0) * X
+    comps = [rho, rho * vx, rho * vy]
+    for s in range(nvar - 3):
+        comps.append(rho * np.where(X + s * 0.1 > 0, 1.0, 0.0))
+    return np.stack(comps, axis=-1)
+
+
+@pytest.mark.parametrize("kind", ["steps", "linear", "tiny"])
+@pytest.mark.parametrize("rec", RECONS)
+def test_limiters_on_ties_zeros_and_subnormals(G, kind, rec):
+    U0 = tie_heavy_state(36, 20, 4, kind)
+    for rs in SOLVERS:
+        args = (1e-3, 1 / 36, 1 / 20, 1.0, 1e-10, "rk3")
+        gpu = G.isothermal_step(U0, *args, reconstruct=rec, rsolver=rs)
+        ref = H.step(U0, *args, recon=rec, solver=rs)
+        assert_rel(gpu, ref, STEP_RTOL, f"{kind} {rec} {rs}")
+        from jathenax_gb300 import fluxes as GF
+        W = H.primitives(U0, 1e-10)[1]
+        for axis in (0, 1):
+            for a, b in zip(GF.reconstruct_faces(W, axis, rec, 1e-10), H.face_states(W, axis, rec, 1e-10)):
+                assert_rel(a, b, STEP_RTOL, f"{kind} {rec} faces axis {axis}")

@@ -91,7 +91,7 @@ def test_oracle_runs_bitwise(golden):
     assert out[3] == g["kh_cycle"]
     x = (np.arange(32) + 0.5) / 32 - 0.5
     tables = F.phase_tables(F.forcing_modes(3, 5, (-5, 5), (-5, 5)), x, x, (1.0, 1.0))
-    out = R.evolve(g["turb_U0"], 1 / 32, 1 / 32, 1.0, 1.17549e-38, "rk3", 0.4, 0.02, 12, nu=1.5e-6,
+    out = R.evolve(g["turb_U0"], 1 / 32, 1 / 32, 1.0, 1.17549e-38, "rk3", 0.4, 0.5, 12, nu=1.5e-6,
                    drag=0.3333335, forcing=(g["turb_table"], tables), dt_update=0.0075, dedt=0.03703705)
     np.testing.assert_array_equal(out[0], g["turb_U"])
     assert out[1] == g["turb_time"] and out[3] == g["turb_cycle"]
