@@ -111,6 +111,20 @@ jx_status jx_timestep(const jx_desc* d, const void* W, double cfl, double prev_d
                       double time, double tlim, double* dt_out, void* workspace,
                       size_t workspace_bytes, jx_stream s);
 
+/* isothermal_timestep without a workspace, for callers that cannot allocate
+ * device memory: e.g. a JAX/XLA FFI handler, where XLA has reserved most of
+ * the GPU and owns every buffer, or a loop with a no-allocation rule. No
+ * counterpart in the reference (which never allocates explicitly).
+ * Same arguments and result as jx_timestep minus the workspace. Its scratch
+ * is a 65,792-byte static device array in libjx.so (2048 CFL partial slots,
+ * enough for every grid jx_check_desc accepts; a grid that needed more would
+ * be refused with JX_ERR_INVALID). The first call on a device looks up the
+ * array's address on that device; make that first call before any stream
+ * capture. Calls share the array: calls whose kernels overlap on the GPU
+ * race. Allocates nothing. */
+jx_status jx_timestep_noalloc(const jx_desc* d, const void* W, double cfl, double prev_dt,
+                              double time, double tlim, double* dt_out, jx_stream s);
+
 /* One RK stage of isothermal_step (hydro.py:101-143) fused into one kernel:
  * reconstruction, Riemann solve, viscous + Smagorinsky + SGS stress, flux
  * divergence, the RK combine (rk_stage, hydro.py:39-51), drag, and the

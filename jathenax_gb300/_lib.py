@@ -73,6 +73,7 @@ PROTOTYPES = {
     "jx_num_stages": [_I32],
     "jx_recover": [_DP, _P, _P, _P, _P],
     "jx_timestep": [_DP, _P, _D, _D, _D, _D, _P, _P, _SZ, _P],
+    "jx_timestep_noalloc": [_DP, _P, _D, _D, _D, _D, _P, _P],
     "jx_stage": [_DP, _I32, _P, _P, _P, _P, _P, _I32, _P, ctypes.POINTER(Trace), _P, _SZ, _P],
     "jx_cfl_partials": [_DP, _P, _P, _SZ, _P],
     "jx_begin_step": [_DP, _P, _I32, _P, _SZ, _P],

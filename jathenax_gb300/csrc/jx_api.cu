@@ -517,3 +517,71 @@ jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sin
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// jx_timestep_noalloc: isothermal_timestep for callers that cannot allocate
+// device memory and have no workspace to pass.
+//
+// Its scratch is g_timestep_scratch below: a file-scope device array that
+// holds the per-block CFL partials and their count. The CFL kernel launches at
+// most kCflBlocksMax blocks and strides over larger grids, so 2048 partial
+// slots (64 KiB + a 256-byte header) cover every grid jx_check_desc accepts.
+// Every GPU that loads libjx.so keeps these 65,792 bytes until the process
+// exits. All calls share the array: each call rewrites every slot it reads
+// (the count included) before reading it, so nothing has to start at zero,
+// but two calls whose kernels overlap on the GPU (different streams, or
+// different host threads) race on the array.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocSlots = jx::kCflBlocksMax;
+constexpr size_t kNoAllocBytes = jx::kWsHeader + kNoAllocSlots * jx::kCflSlots * sizeof(double);
+static __device__ __align__(256) unsigned char g_timestep_scratch[kNoAllocBytes];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_address[64] = {};  // device address of g_timestep_scratch, per device
+
+// The array's host-side name is not a device address; look the address up
+// once per device, with that device current.
+jx_status scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(JX_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(JX_ERR_INVALID, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_address[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_timestep_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(JX_ERR_CUDA, "cudaGetSymbolAddress(timestep scratch): %s", cudaGetErrorString(e));
+    g_scratch_address[dev] = p;
+  }
+  *out = g_scratch_address[dev];
+  return JX_OK;
+}
+
+}  // namespace
+
+extern "C" jx_status jx_timestep_noalloc(const jx_desc* d, const void* W, double cfl, double prev_dt,
+                                         double time, double tlim, double* dt_out, jx_stream s) {
+  jx_status st = check_desc(d);
+  if (st) return st;
+  if (!W || !dt_out) return fail(JX_ERR_INVALID, "null W or dt_out");
+  const int64_t ncell = (int64_t)d->ny * d->nx;
+  const size_t need = kWsHeader + (size_t)cfl_grid(ncell) * kCflSlots * sizeof(double);
+  if (need > kNoAllocBytes)
+    return fail(JX_ERR_INVALID, "grid of %lld cells needs %zu bytes of timestep scratch; the static scratch holds %zu",
+                (long long)ncell, need, kNoAllocBytes);
+  void* base = nullptr;
+  if ((st = scratch_address(&base))) return st;
+  Ws w;
+  w.header = static_cast<WsHeader*>(base);
+  w.cfl = reinterpret_cast<double*>(static_cast<char*>(base) + kWsHeader);
+  CflParams q = cfl_params(d, W, nullptr, w);
+  if ((st = cuda_check(launch_cfl(d->dtype, true, q, (cudaStream_t)s), "cfl kernel"))) return st;
+  return cuda_check(launch_timestep_finish(dt_params(d), w.cfl, w.header, prev_dt, time, tlim, cfl, dt_out,
+                                           (cudaStream_t)s),
+                    "timestep finisher");
+}
