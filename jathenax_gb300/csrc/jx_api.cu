@@ -78,7 +78,9 @@ jx_status check_desc(const jx_desc* d) {
 
 struct Tile {
   int tx, ty, tiles_x, tiles_y;
-  size_t smem;
+  size_t smem;       // generic kernel
+  bool fast_shape;   // 3/4 variables at tile width 32: the fast kernel applies
+  size_t fast_smem;  // fast kernel
 };
 
 jx_status resolve_tile(const jx_desc* d, Tile* t) {
@@ -97,6 +99,11 @@ jx_status resolve_tile(const jx_desc* d, Tile* t) {
   }
   if (smem > kSmemLimit)
     return fail(JX_ERR_INVALID, "tile %dx%d needs %zu bytes of shared memory (limit %zu)", tx, ty, smem, kSmemLimit);
+  t->fast_shape = (d->nvar == 3 || d->nvar == 4) && tx == 32;
+  t->fast_smem = t->fast_shape ? fast_smem_bytes(d->recon, d->dtype, ty) : 0;
+  if (t->fast_smem > kSmemLimit)
+    return fail(JX_ERR_INVALID, "tile 32x%d needs %zu bytes of shared memory (limit %zu)", ty, t->fast_smem,
+                kSmemLimit);
   t->tx = tx;
   t->ty = ty;
   t->tiles_x = (d->nx + tx - 1) / tx;
@@ -179,8 +186,22 @@ CflParams cfl_params(const jx_desc* d, const void* X, const jx_clock* clock, con
   return q;
 }
 
+bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 cudaError_t launch_stage(const jx_desc* d, const StageParams& p, const Tile& t, cudaStream_t s) {
   dim3 grid((unsigned)((int64_t)t.tiles_x * t.tiles_y));
+  // The fast kernel reads/writes 4-variable cells with 128-bit accesses.
+  const bool fast = t.fast_shape && (d->nvar == 3 || (aligned16(p.U) && aligned16(p.V) && aligned16(p.Uout) &&
+                                                      (p.Vout == nullptr || aligned16(p.Vout))));
+  if (fast) {
+    switch (d->recon) {
+      case JX_DC: return launch_fast_dc(d->dtype, d->rsolver, p, grid, t.fast_smem, s);
+      case JX_PLM: return launch_fast_plm(d->dtype, d->rsolver, p, grid, t.fast_smem, s);
+      case JX_PPM4: return launch_fast_ppm4(d->dtype, d->rsolver, p, grid, t.fast_smem, s);
+      case JX_PPMX: return launch_fast_ppmx(d->dtype, d->rsolver, p, grid, t.fast_smem, s);
+      default: return launch_fast_wenoz(d->dtype, d->rsolver, p, grid, t.fast_smem, s);
+    }
+  }
   switch (d->recon) {
     case JX_DC: return launch_stage_dc(d->dtype, d->rsolver, p, grid, t.smem, s);
     case JX_PLM: return launch_stage_plm(d->dtype, d->rsolver, p, grid, t.smem, s);

@@ -82,6 +82,24 @@ cudaError_t launch_stage_ppm4(int, int, const StageParams&, dim3, size_t, cudaSt
 cudaError_t launch_stage_ppmx(int, int, const StageParams&, dim3, size_t, cudaStream_t);
 cudaError_t launch_stage_wenoz(int, int, const StageParams&, dim3, size_t, cudaStream_t);
 
+cudaError_t launch_fast_dc(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+cudaError_t launch_fast_plm(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+cudaError_t launch_fast_ppm4(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+cudaError_t launch_fast_ppmx(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+cudaError_t launch_fast_wenoz(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+
+// Shared memory of the 3/4-variable fast stage kernel (tile width 32): the
+// same planes as the generic kernel, stored as 4-wide cell vectors.
+inline size_t fast_smem_bytes(int recon, int dtype, int ty) {
+  const int h = recon == JX_DC ? 1 : (recon == JX_PLM ? 2 : 3);
+  const size_t tx = 32;
+  const size_t w = (tx + 2 * h) * (size_t)(ty + 2 * h), fx = (size_t)ty * (tx + 1), fy = (size_t)(ty + 1) * tx;
+  const size_t ax = (size_t)ty * (tx + 3), ay = (size_t)(ty + 3) * tx;
+  const size_t a = (recon == JX_PPM4 || recon == JX_PPMX) ? (ax > ay ? ax : ay) : 0;
+  const size_t r = fx > fy ? fx : fy;
+  return (w + fx + fy + a + r) * 4 * (dtype == JX_F64 ? 8 : 4);
+}
+
 typedef cudaError_t (*FaceStatesLauncher)(int dtype, const void* W, int ny, int nx, int nv,
                                           int axis, double dfloor, void* left, void* right,
                                           cudaStream_t s);

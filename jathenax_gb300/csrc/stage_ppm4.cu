@@ -1,7 +1,8 @@
-// Stage-kernel instantiations for the ppm4 reconstruction (float64 and
+// Stage-kernel instantiations (generic and 3/4-variable fast path) for the ppm4 reconstruction (float64 and
 // float32, all three Riemann solvers). One file per reconstruction keeps
 // the per-file compile short and lets the build run them in parallel.
 #include "jx_stage.cuh"
+#include "jx_stage_fast.cuh"
 
 namespace jx {
 cudaError_t launch_stage_ppm4(int dtype, int rsolver, const StageParams& p, dim3 grid, size_t smem,
@@ -11,5 +12,9 @@ cudaError_t launch_stage_ppm4(int dtype, int rsolver, const StageParams& p, dim3
 cudaError_t face_states_ppm4(int dtype, const void* W, int ny, int nx, int nv, int axis, double dfloor,
                            void* left, void* right, cudaStream_t s) {
   return launch_face_states_recon<JX_PPM4>(dtype, W, ny, nx, nv, axis, dfloor, left, right, s);
+}
+cudaError_t launch_fast_ppm4(int dtype, int rsolver, const StageParams& p, dim3 grid, size_t smem,
+                           cudaStream_t s) {
+  return launch_fast_recon<JX_PPM4>(dtype, rsolver, p, grid, smem, s);
 }
 }  // namespace jx

@@ -299,3 +299,25 @@ def test_limiters_on_ties_zeros_and_subnormals(G, kind, rec):
         for axis in (0, 1):
             for a, b in zip(GF.reconstruct_faces(W, axis, rec, 1e-10), H.face_states(W, axis, rec, 1e-10)):
                 assert_rel(a, b, STEP_RTOL, f"{kind} {rec} faces axis {axis}")
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_unaligned_state_pointers_use_the_generic_kernel(G, dtype):
+    """4-variable states that are not 16-byte aligned take the scalar-access kernel."""
+    import torch
+    from jathenax_gb300 import _lib
+    U0 = noisy_state(40, 24, nvar=4, seed=13)
+    ref = H.step(U0, 0.001, 1 / 40, 1 / 24, 1.0, 1e-10, "rk3")
+    tdtype = getattr(torch, dtype)
+    n = U0.size
+    # Views starting one element into larger buffers: 8- or 4-byte aligned only.
+    bufs = [torch.zeros(n + 1, dtype=tdtype, device="cuda") for _ in range(3)]
+    U_in, A, B = (b[1:].view(U0.shape) for b in bufs)
+    U_in.copy_(torch.as_tensor(U0, device="cuda"))
+    assert U_in.data_ptr() % 16 != 0
+    desc = G.make_desc(U0.shape, tdtype, 1 / 40, 1 / 24, 1.0, 1e-10, "rk3")
+    ws, nbytes = _lib.workspace(desc)
+    clock = _lib.new_clock(dt=0.001)
+    out, _ = G.run_stages(desc, U_in, clock=clock, ws=ws, nbytes=nbytes, out=A)
+    tol = STEP_RTOL if dtype == "float64" else 1e-5
+    assert_rel(out.cpu().numpy(), ref, tol)
