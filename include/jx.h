@@ -173,6 +173,35 @@ jx_status jx_force_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock
 jx_status jx_step(const jx_desc* d, void* S, void* A, void* B, const jx_forcing* forcing,
                   jx_clock* clock, void* workspace, size_t workspace_bytes, jx_stream s);
 
+/* One solve of a batch: the arguments of jx_step. forcing.raw_force == NULL
+ * means unforced. */
+typedef struct {
+  jx_desc desc;
+  void *S, *A, *B;
+  jx_clock* clock;
+  jx_forcing forcing;
+  void* workspace;
+  size_t workspace_bytes;
+} jx_solve;
+
+/* Batches advance many independent solves together (the reference evolves
+ * one grid per evolve_isothermal call, run.py:20-69): per RK stage one
+ * persistent launch per (precision, reconstruction, Riemann solver) group
+ * walks a tile work list spanning all the group's grids. Solves must have 3
+ * or 4 variables (16-byte aligned states for 4); tiles are 32 x tile_y and
+ * each workspace must be sized for that tile (desc.tile_x = 32,
+ * desc.tile_y = tile_y in jx_workspace_bytes). Results are bitwise the same
+ * as running each solve alone with jx_step at the same tile.
+ * jx_batch_plan writes a plan into host memory; copy it unchanged to device
+ * memory of the same size and pass both to jx_batch_step, which enqueues one
+ * evolve cycle of every solve (batched begin-step, renders, stages, kicks).
+ * blocks_per_sm <= 0 picks the occupancy limit. */
+jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, int32_t tile_y, size_t* bytes);
+jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void* plan, size_t bytes);
+jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_per_sm, jx_stream s);
+/* Number of launch groups in a plan (-1 if not a plan). */
+int32_t jx_batch_groups(const void* plan);
+
 /* rk_stage (hydro.py:39-51) on whole arrays: U_out = combine(U, V, div),
  * V_out = V + delta*U when has_delta. n = number of elements. */
 jx_status jx_rk_stage(int32_t dtype, int64_t n, const void* U, const void* V, const void* div,

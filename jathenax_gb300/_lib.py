@@ -59,6 +59,12 @@ class Trace(ctypes.Structure):
         "saved", "conserved", "before_kick", "acceleration")]
 
 
+class SolveStruct(ctypes.Structure):
+    _fields_ = [("desc", Desc), ("S", ctypes.c_void_p), ("A", ctypes.c_void_p), ("B", ctypes.c_void_p),
+                ("clock", ctypes.c_void_p), ("forcing", Forcing), ("workspace", ctypes.c_void_p),
+                ("workspace_bytes", ctypes.c_size_t)]
+
+
 assert ctypes.sizeof(Clock) == 128
 
 _P, _I32, _I64, _D, _SZ = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_size_t
@@ -89,9 +95,13 @@ PROTOTYPES = {
     "jx_box_sums": [_DP, _P, _P, _P, _SZ, _P],
     "jx_tile_info": [_DP, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
     "jx_probe_fma": [_I32, _I32, _I32, _P, _P],
+    "jx_batch_plan_bytes": [ctypes.POINTER(SolveStruct), _I32, _I32, ctypes.POINTER(_SZ)],
+    "jx_batch_plan": [ctypes.POINTER(SolveStruct), _I32, _I32, _P, _SZ],
+    "jx_batch_step": [_P, _P, _I32, _P],
+    "jx_batch_groups": [_P],
 }
 _RESTYPES = {"jx_last_error": ctypes.c_char_p, "jx_version": ctypes.c_char_p,
-             "jx_num_stages": ctypes.c_int32}
+             "jx_num_stages": ctypes.c_int32, "jx_batch_groups": ctypes.c_int32}
 
 _lib = None
 

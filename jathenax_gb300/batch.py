@@ -1,0 +1,95 @@
+"""Batches: many independent device-resident solves advanced together.
+
+Per RK stage, one persistent launch per (precision, reconstruction, Riemann
+solver) group walks a tile work list spanning every grid of the group; the
+batched begin-step kernel picks each solve's own dt; forced solves get their
+own render/normalise/kick launches. A whole cycle is enqueued by one
+``jx_batch_step`` call and can be captured in a CUDA graph. Each solve keeps
+its own clock, workspace and CFL partials (one slot per tile), so a solve's
+result is bitwise the same alone and in any batch.
+"""
+
+import ctypes
+
+from . import _lib
+
+
+class ClockBank:
+    """One device buffer holding the 128-byte clocks of many solves."""
+
+    def __init__(self, n):
+        t = _lib.torch()
+        self.buf = t.zeros((n, 128), dtype=t.uint8, device=_lib.device())
+
+    def slot(self, i):
+        return self.buf[i]
+
+    def read(self):
+        raw = self.buf.cpu().numpy()
+        return [_lib.Clock.from_buffer_copy(raw[i].tobytes()) for i in range(raw.shape[0])]
+
+
+class Batch:
+    """Advance a list of :class:`jathenax_gb300.solver.Solve` together.
+
+    All solves must use the same tile (``tile=(32, tile_y)`` at construction)
+    and have 3 or 4 variables.
+    """
+
+    def __init__(self, solves, blocks_per_sm=0, clocks=None):
+        t = _lib.torch()
+        self.solves = list(solves)
+        if not self.solves:
+            raise ValueError("a batch needs at least one solve")
+        tiles = {(s.desc.tile_x or 32, s.desc.tile_y or 16) for s in self.solves}
+        if len(tiles) != 1 or next(iter(tiles))[0] != 32:
+            raise ValueError("batched solves must share one 32 x tile_y tile")
+        self.tile_y = next(iter(tiles))[1]
+        self.blocks_per_sm = int(blocks_per_sm)
+        self.clocks = clocks
+        n = len(self.solves)
+        arr = (_lib.SolveStruct * n)(*[s.as_jx_solve() for s in self.solves])
+        size = ctypes.c_size_t()
+        _lib.call("jx_batch_plan_bytes", arr, n, self.tile_y, ctypes.byref(size))
+        self.plan_host = t.empty(int(size.value), dtype=t.uint8).pin_memory()
+        _lib.call("jx_batch_plan", arr, n, self.tile_y, ctypes.c_void_p(self.plan_host.data_ptr()), size.value)
+        self.plan_dev = self.plan_host.to(_lib.device(), non_blocking=False)
+        self.groups = _lib.load().jx_batch_groups(ctypes.c_void_p(self.plan_host.data_ptr()))
+        self.graph = None
+
+    def enqueue_step(self):
+        """Enqueue one cycle of every solve on the current stream."""
+        _lib.call("jx_batch_step", ctypes.c_void_p(self.plan_host.data_ptr()),
+                  ctypes.c_void_p(self.plan_dev.data_ptr()), self.blocks_per_sm, _lib.stream_handle())
+
+    def capture(self, steps):
+        """Capture `steps` cycles in a CUDA graph (call after one eager step)."""
+        t = _lib.torch()
+        t.cuda.synchronize()
+        graph = t.cuda.CUDAGraph()
+        with t.cuda.graph(graph):
+            for _ in range(steps):
+                self.enqueue_step()
+        self.graph, self.graph_steps = graph, steps
+
+    def states(self):
+        if self.clocks is not None:
+            return self.clocks.read()
+        return [s.state() for s in self.solves]
+
+    def run(self, steps_per_sync=16, use_graph=True):
+        """Advance until every solve reached its tlim or nlim; returns the clocks."""
+        self.enqueue_step()
+        if all(c.done for c in self.states()):
+            return self.states()
+        if use_graph and self.graph is None:
+            self.capture(steps_per_sync)
+        while True:
+            if use_graph:
+                self.graph.replay()
+            else:
+                for _ in range(steps_per_sync):
+                    self.enqueue_step()
+            clocks = self.states()
+            if all(c.done for c in clocks):
+                return clocks

@@ -5,6 +5,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <vector>
+
 #include "jx_aux.cuh"
 #include "jx_internal.h"
 
@@ -211,15 +213,12 @@ cudaError_t launch_stage(const jx_desc* d, const StageParams& p, const Tile& t, 
   }
 }
 
-jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, const void* U_in,
-                   const void* V_in, void* U_out, void* V_out, const void* tau, int force_follows,
-                   jx_clock* clock, const jx_trace* trace, cudaStream_t s) {
+// Launch parameters of one stage (hydro.py:101-143); validated by the caller.
+StageParams make_stage_params(const jx_desc* d, const Tile& t, const Ws& w, int stage, const void* U_in,
+                              const void* V_in, void* U_out, void* V_out, const void* tau, int force_follows,
+                              jx_clock* clock, const jx_trace* trace) {
   const int n = jx_num_stages(d->integrator);
-  if (stage < 1 || stage > n) return fail(JX_ERR_INVALID, "stage %d outside 1..%d", stage, n);
-  if (!U_in || !V_in || !U_out || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
   const RkRow& row = rk_rows(d->integrator)[stage - 1];
-  if (U_in == U_out || (row.has_delta && U_in == V_out))
-    return fail(JX_ERR_INVALID, "U_in must not alias an output");
   const bool last = stage == n;
   StageParams p;
   memset(&p, 0, sizeof(p));
@@ -264,6 +263,20 @@ jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, cons
   p.drag_on = d->drag_rate > 0.0;
   fill_stage_consts(p.cd, p);
   fill_stage_consts(p.cf, p);
+  return p;
+}
+
+jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, const void* U_in,
+                   const void* V_in, void* U_out, void* V_out, const void* tau, int force_follows,
+                   jx_clock* clock, const jx_trace* trace, cudaStream_t s) {
+  const int n = jx_num_stages(d->integrator);
+  if (stage < 1 || stage > n) return fail(JX_ERR_INVALID, "stage %d outside 1..%d", stage, n);
+  if (!U_in || !V_in || !U_out || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
+  const RkRow& row = rk_rows(d->integrator)[stage - 1];
+  if (U_in == U_out || (row.has_delta && U_in == V_out))
+    return fail(JX_ERR_INVALID, "U_in must not alias an output");
+  const StageParams p =
+      make_stage_params(d, t, w, stage, U_in, V_in, U_out, V_out, tau, force_follows, clock, trace);
   return cuda_check(launch_stage(d, p, t, s), "stage kernel");
 }
 
@@ -535,6 +548,271 @@ jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sin
   if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
   if (blocks < 1 || iters < 1 || !sink) return fail(JX_ERR_INVALID, "bad probe arguments");
   return cuda_check(launch_probe(dtype, blocks, iters, sink, (cudaStream_t)s), "probe kernel");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many solves advanced together, one persistent stage launch per
+// (precision, reconstruction, Riemann solver) group and RK stage.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kPlanMagic = 0x4a584250;  // "JXBP"
+constexpr int kMaxGroups = 30;
+
+struct BatchGroup {
+  int dtype, recon, rsolver, first, count, tile_first, nwork, pad;
+  size_t smem;
+};
+
+struct BatchSolveInfo {
+  jx_solve solve;  // with desc.tile_x/tile_y set to the plan's tile
+  int forced, smag, n_stages, pad;
+};
+
+struct BatchPlanHeader {
+  uint32_t magic;
+  int32_t n, n_groups, max_stages, tile_y, pad;
+  int64_t bytes, off_params, off_offsets, off_begin, off_info;
+  BatchGroup groups[kMaxGroups];
+};
+
+struct PlanLayout {
+  size_t params, offsets, begin, info, total;
+};
+
+PlanLayout plan_layout(int n) {
+  PlanLayout L;
+  size_t off = align256(sizeof(BatchPlanHeader));
+  L.params = off;
+  off = align256(off + (size_t)4 * n * sizeof(StageParams));
+  L.offsets = off;
+  off = align256(off + (size_t)(n + kMaxGroups) * sizeof(int));
+  L.begin = off;
+  off = align256(off + (size_t)n * sizeof(BeginParams));
+  L.info = off;
+  off = align256(off + (size_t)n * sizeof(BatchSolveInfo));
+  L.total = off;
+  return L;
+}
+
+int sm_count() {
+  static int sms[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (!sms[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = v > 0 ? v : 1;
+  }
+  return sms[dev];
+}
+
+int batch_occupancy(int recon, int dtype, int rsolver, size_t smem) {
+  switch (recon) {
+    case JX_DC: return batch_blocks_per_sm_dc(dtype, rsolver, smem);
+    case JX_PLM: return batch_blocks_per_sm_plm(dtype, rsolver, smem);
+    case JX_PPM4: return batch_blocks_per_sm_ppm4(dtype, rsolver, smem);
+    case JX_PPMX: return batch_blocks_per_sm_ppmx(dtype, rsolver, smem);
+    default: return batch_blocks_per_sm_wenoz(dtype, rsolver, smem);
+  }
+}
+
+cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* params, const int* offsets,
+                         int nsolves, int nwork, dim3 grid, size_t smem, cudaStream_t s) {
+  switch (recon) {
+    case JX_DC: return launch_batch_dc(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+    case JX_PLM: return launch_batch_plm(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+    case JX_PPM4: return launch_batch_ppm4(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+    case JX_PPMX: return launch_batch_ppmx(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+    default: return launch_batch_wenoz(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+  }
+}
+
+jx_status check_batch_solve(int i, const jx_solve& in, int tile_y, jx_solve* out, Tile* t, Ws* w) {
+  *out = in;
+  out->desc.tile_x = 32;
+  out->desc.tile_y = tile_y;
+  jx_status st = check_desc(&out->desc);
+  if (st) return fail(st, "solve %d: %s", i, jx_last_error());
+  const jx_desc& d = out->desc;
+  if (d.nvar != 3 && d.nvar != 4) return fail(JX_ERR_INVALID, "solve %d: batches take 3 or 4 variables", i);
+  if (!in.S || !in.A || !in.B || !in.clock) return fail(JX_ERR_INVALID, "solve %d: null state or clock", i);
+  if (in.S == in.A || in.S == in.B || in.A == in.B) return fail(JX_ERR_INVALID, "solve %d: S, A, B must differ", i);
+  if (d.nvar == 4 && !(aligned16(in.S) && aligned16(in.A) && aligned16(in.B)))
+    return fail(JX_ERR_INVALID, "solve %d: 4-variable states must be 16-byte aligned", i);
+  if ((st = resolve_tile(&d, t))) return fail(st, "solve %d: %s", i, jx_last_error());
+  if ((st = bind_ws(&d, *t, in.workspace, in.workspace_bytes, w))) return fail(st, "solve %d: %s", i, jx_last_error());
+  if (in.forcing.raw_force && (!in.forcing.table || !in.forcing.cos_x || !in.forcing.sin_x || !in.forcing.cos_y ||
+                               !in.forcing.sin_y || in.forcing.n_modes < 1 || in.forcing.n_updates < 1))
+    return fail(JX_ERR_INVALID, "solve %d: incomplete forcing tables", i);
+  return JX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, int32_t tile_y, size_t* bytes) {
+  if (!solves || n < 1 || !bytes) return fail(JX_ERR_INVALID, "a batch needs at least one solve");
+  if (tile_y < 1 || tile_y > 64) return fail(JX_ERR_INVALID, "tile_y must be in [1, 64]");
+  *bytes = plan_layout(n).total;
+  return JX_OK;
+}
+
+jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void* plan, size_t bytes) {
+  size_t need = 0;
+  jx_status st = jx_batch_plan_bytes(solves, n, tile_y, &need);
+  if (st) return st;
+  if (!plan || bytes < need) return fail(JX_ERR_WORKSPACE, "plan buffer has %zu bytes, needs %zu", bytes, need);
+  const PlanLayout L = plan_layout(n);
+  char* base = static_cast<char*>(plan);
+  memset(base, 0, need);
+  BatchPlanHeader* h = reinterpret_cast<BatchPlanHeader*>(base);
+  h->magic = kPlanMagic;
+  h->n = n;
+  h->tile_y = tile_y;
+  h->bytes = (int64_t)need;
+  h->off_params = (int64_t)L.params;
+  h->off_offsets = (int64_t)L.offsets;
+  h->off_begin = (int64_t)L.begin;
+  h->off_info = (int64_t)L.info;
+  StageParams* params = reinterpret_cast<StageParams*>(base + L.params);
+  int* offsets = reinterpret_cast<int*>(base + L.offsets);
+  BeginParams* begin = reinterpret_cast<BeginParams*>(base + L.begin);
+  BatchSolveInfo* info = reinterpret_cast<BatchSolveInfo*>(base + L.info);
+
+  // Validate every solve once, then group by (precision, reconstruction,
+  // Riemann solver) in order of first appearance; solves keep their relative
+  // order inside a group.
+  std::vector<jx_solve> sv(n);
+  std::vector<Tile> tl(n);
+  std::vector<Ws> wl(n);
+  for (int i = 0; i < n; ++i)
+    if ((st = check_batch_solve(i, solves[i], tile_y, &sv[i], &tl[i], &wl[i]))) return st;
+  std::vector<int> group_of(n, -1);
+  int n_groups = 0;
+  for (int i = 0; i < n; ++i) {
+    const jx_desc& d = sv[i].desc;
+    int g = 0;
+    while (g < n_groups && !(h->groups[g].dtype == d.dtype && h->groups[g].recon == d.recon &&
+                             h->groups[g].rsolver == d.rsolver))
+      ++g;
+    if (g == n_groups) {
+      if (n_groups == kMaxGroups) return fail(JX_ERR_INVALID, "more than %d solver groups", kMaxGroups);
+      BatchGroup& G = h->groups[n_groups++];
+      G.dtype = d.dtype;
+      G.recon = d.recon;
+      G.rsolver = d.rsolver;
+      G.smem = fast_smem_bytes(d.recon, d.dtype, tile_y);
+    }
+    group_of[i] = g;
+  }
+  int order_count = 0, next_int = 0;
+  for (int g = 0; g < n_groups; ++g) {
+    BatchGroup& G = h->groups[g];
+    G.first = order_count;
+    G.tile_first = next_int;
+    int tiles = 0;
+    for (int i = 0; i < n; ++i) {
+      if (group_of[i] != g) continue;
+      const jx_desc& d = sv[i].desc;
+      const Tile& t = tl[i];
+      const Ws& w = wl[i];
+      const int k = order_count++;
+      const int nst = jx_num_stages(d.integrator);
+      const bool forced = sv[i].forcing.raw_force != nullptr;
+      BatchSolveInfo& I = info[k];
+      I.solve = sv[i];
+      I.forced = forced;
+      I.smag = d.smagorinsky_cs > 0.0;
+      I.n_stages = nst;
+      if (nst > h->max_stages) h->max_stages = nst;
+      offsets[next_int++] = tiles;
+      tiles += t.tiles_x * t.tiles_y;
+      BeginParams& B = begin[k];
+      B.q = dt_params(&d);
+      B.clock = sv[i].clock;
+      B.partials = w.cfl;
+      B.header = w.header;
+      B.forced = forced;
+      const void* in = sv[i].S;
+      for (int stage = 1; stage <= 4; ++stage) {
+        StageParams& P = params[(size_t)(stage - 1) * n + k];
+        if (stage > nst) {
+          memset(&P, 0, sizeof(P));
+          P.skip = 1;
+          P.clock = sv[i].clock;
+          continue;
+        }
+        void* out = stage == nst ? sv[i].S : (stage % 2 == 1 ? sv[i].A : sv[i].B);
+        P = make_stage_params(&d, t, w, stage, in, sv[i].S, out, stage == nst ? nullptr : sv[i].S, nullptr,
+                              forced, sv[i].clock, nullptr);
+        in = out;
+      }
+    }
+    offsets[next_int++] = tiles;
+    G.count = order_count - G.first;
+    G.nwork = tiles;
+  }
+  h->n_groups = n_groups;
+  return JX_OK;
+}
+
+jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_per_sm, jx_stream stream) {
+  const BatchPlanHeader* h = static_cast<const BatchPlanHeader*>(plan);
+  if (!h || !plan_dev || h->magic != kPlanMagic) return fail(JX_ERR_INVALID, "not a batch plan");
+  cudaStream_t s = (cudaStream_t)stream;
+  const char* base = static_cast<const char*>(plan);
+  const char* dbase = static_cast<const char*>(plan_dev);
+  const BatchSolveInfo* info = reinterpret_cast<const BatchSolveInfo*>(base + h->off_info);
+  const StageParams* params_dev = reinterpret_cast<const StageParams*>(dbase + h->off_params);
+  const int* offsets_dev = reinterpret_cast<const int*>(dbase + h->off_offsets);
+  const BeginParams* begin_dev = reinterpret_cast<const BeginParams*>(dbase + h->off_begin);
+  jx_status st;
+  if ((st = cuda_check(launch_begin_step_batch(begin_dev, h->n, s), "batched begin-step kernel"))) return st;
+  for (int i = 0; i < h->n; ++i)
+    if (info[i].forced && (st = jx_force_render(&info[i].solve.desc, &info[i].solve.forcing, info[i].solve.clock,
+                                                stream)))
+      return st;
+  const int sms = sm_count();
+  for (int stage = 1; stage <= h->max_stages; ++stage) {
+    for (int g = 0; g < h->n_groups; ++g) {
+      const BatchGroup& G = h->groups[g];
+      int bps = blocks_per_sm;
+      if (bps <= 0) bps = batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
+      if (bps < 1) bps = 1;
+      int64_t blocks = (int64_t)sms * bps;
+      if (blocks > G.nwork) blocks = G.nwork;
+      if (blocks < 1) continue;
+      if ((st = cuda_check(launch_batch(G.recon, G.dtype, G.rsolver, params_dev + (size_t)(stage - 1) * h->n + G.first,
+                                        offsets_dev + G.tile_first, G.count, G.nwork, dim3((unsigned)blocks), G.smem,
+                                        s),
+                           "batched stage kernel")))
+        return st;
+    }
+  }
+  for (int i = 0; i < h->n; ++i) {
+    const jx_solve& sv = info[i].solve;
+    if (!info[i].forced && !info[i].smag) continue;
+    Tile t;
+    Ws w;
+    if ((st = resolve_tile(&sv.desc, &t)) || (st = bind_ws(&sv.desc, t, sv.workspace, sv.workspace_bytes, &w)))
+      return st;
+    if (info[i].forced && (st = do_kick(&sv.desc, &sv.forcing, sv.S, sv.clock, nullptr, w, s))) return st;
+    if (info[i].smag) {
+      CflParams q = cfl_params(&sv.desc, sv.S, sv.clock, w);
+      if ((st = cuda_check(launch_cfl(sv.desc.dtype, false, q, s), "cfl kernel"))) return st;
+    }
+  }
+  return JX_OK;
+}
+
+int32_t jx_batch_groups(const void* plan) {
+  const BatchPlanHeader* h = static_cast<const BatchPlanHeader*>(plan);
+  return h && h->magic == kPlanMagic ? h->n_groups : -1;
 }
 
 }  // extern "C"

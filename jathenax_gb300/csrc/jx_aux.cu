@@ -48,8 +48,8 @@ __device__ void reduce_cfl_partials(const double* partials, int64_t n, double ou
 
 // run.py:40-53 for one cycle: commit the previous cycle, test the loop
 // condition, choose dt, update the forcing schedule (forcing.py:125-134).
-__global__ void begin_step_kernel(DtParams q, jx_clock* clock, const double* partials,
-                                  const WsHeader* hdr, int forced) {
+__device__ void begin_step_body(const DtParams& q, jx_clock* clock, const double* partials, const WsHeader* hdr,
+                                int forced) {
   __shared__ double red[32 * 3];
   __shared__ int stop;
   if (threadIdx.x == 0) {
@@ -83,6 +83,17 @@ __global__ void begin_step_kernel(DtParams q, jx_clock* clock, const double* par
       clock->power = clock->update >= 0 ? clock->dedt : 0.0;
     }
   }
+}
+
+__global__ void begin_step_kernel(DtParams q, jx_clock* clock, const double* partials, const WsHeader* hdr,
+                                  int forced) {
+  begin_step_body(q, clock, partials, hdr, forced);
+}
+
+// One block per solve of a batch.
+__global__ void begin_step_batch_kernel(const BeginParams* __restrict__ solves) {
+  const BeginParams& b = solves[blockIdx.x];
+  begin_step_body(b.q, b.clock, b.partials, b.header, b.forced);
 }
 
 // isothermal_timestep on caller-given W and host scalars.
@@ -584,6 +595,12 @@ __global__ void fma_probe_kernel(int iters, double* sink) {
 cudaError_t launch_begin_step(const DtParams& q, jx_clock* clock, const double* partials,
                               const WsHeader* hdr, int forced, cudaStream_t s) {
   begin_step_kernel<<<1, kReduceThreads, 0, s>>>(q, clock, partials, hdr, forced);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_begin_step_batch(const BeginParams* solves, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  begin_step_batch_kernel<<<n, kReduceThreads, 0, s>>>(solves);
   return cudaGetLastError();
 }
 

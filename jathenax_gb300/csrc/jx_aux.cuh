@@ -9,6 +9,14 @@ struct DtParams {
   double dx, dy, nu, smag_cs, smag_c, drag;
 };
 
+struct BeginParams {
+  DtParams q;
+  jx_clock* clock;
+  const double* partials;
+  const WsHeader* header;
+  int forced, pad;
+};
+
 struct CflParams {
   const void* X;  // U (conserved) or W (primitives)
   const jx_clock* clock;  // may be null
@@ -44,6 +52,7 @@ struct ForceParams {
 
 cudaError_t launch_begin_step(const DtParams& q, jx_clock* clock, const double* partials,
                               const WsHeader* hdr, int forced, cudaStream_t s);
+cudaError_t launch_begin_step_batch(const BeginParams* solves, int n, cudaStream_t s);
 cudaError_t launch_timestep_finish(const DtParams& q, const double* partials, const WsHeader* hdr,
                                    double prev_dt, double time, double tlim, double cfl,
                                    double* dt_out, cudaStream_t s);

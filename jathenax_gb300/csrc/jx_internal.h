@@ -48,6 +48,7 @@ struct StageParams {
   StageConsts<double> cd;
   StageConsts<float> cf;
   int has_delta, blend, floor_v, floor_out, want_cfl, visc_on, smag_on, drag_on, trace_on;
+  int skip;  // batch only: this solve has no such stage
 };
 
 template <typename R> __host__ __device__ inline const StageConsts<R>& stage_consts(const StageParams& p);
@@ -87,6 +88,17 @@ cudaError_t launch_fast_plm(int, int, const StageParams&, dim3, size_t, cudaStre
 cudaError_t launch_fast_ppm4(int, int, const StageParams&, dim3, size_t, cudaStream_t);
 cudaError_t launch_fast_ppmx(int, int, const StageParams&, dim3, size_t, cudaStream_t);
 cudaError_t launch_fast_wenoz(int, int, const StageParams&, dim3, size_t, cudaStream_t);
+
+cudaError_t launch_batch_dc(int, int, const StageParams*, const int*, int, int, dim3, size_t, cudaStream_t);
+cudaError_t launch_batch_plm(int, int, const StageParams*, const int*, int, int, dim3, size_t, cudaStream_t);
+cudaError_t launch_batch_ppm4(int, int, const StageParams*, const int*, int, int, dim3, size_t, cudaStream_t);
+cudaError_t launch_batch_ppmx(int, int, const StageParams*, const int*, int, int, dim3, size_t, cudaStream_t);
+cudaError_t launch_batch_wenoz(int, int, const StageParams*, const int*, int, int, dim3, size_t, cudaStream_t);
+int batch_blocks_per_sm_dc(int dtype, int rsolver, size_t smem);
+int batch_blocks_per_sm_plm(int dtype, int rsolver, size_t smem);
+int batch_blocks_per_sm_ppm4(int dtype, int rsolver, size_t smem);
+int batch_blocks_per_sm_ppmx(int dtype, int rsolver, size_t smem);
+int batch_blocks_per_sm_wenoz(int dtype, int rsolver, size_t smem);
 
 // Shared memory of the 3/4-variable fast stage kernel (tile width 32): the
 // same planes as the generic kernel, stored as 4-wide cell vectors.

@@ -252,21 +252,21 @@ __device__ __forceinline__ void fast_sweep(const StageParams& p, const StageCons
   (void)nlines;
 }
 
+// One 32 x TY tile of one solve. `tile` indexes the solve's tiles (row-major);
+// its CFL partial goes to slot `tile` of the solve's workspace, so results do
+// not depend on which block or launch processes the tile.
 template <typename R, int RECON, int RS, int NV>
-__global__ void __launch_bounds__(kStageThreads) stage_kernel_fast(const StageParams p) {
-  if (p.clock->done) return;
+__device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int ntiles, unsigned char* smem_raw,
+                                          double* red, R* s_sdt) {
   using N = Num<R>;
   constexpr int H = ReconTraits<RECON>::kHalo;
   constexpr int TX = kFastTX;
   constexpr int PW = TX + 2 * H;
   const StageConsts<R>& k = stage_consts<R>(p);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[32 * 2];
-  __shared__ R s_sdt;
 
   const int tid = threadIdx.x;
   const int TY = p.ty;
-  const int bx = blockIdx.x % p.tiles_x, by = blockIdx.x / p.tiles_x;
+  const int bx = tile % p.tiles_x, by = tile / p.tiles_x;
   const int x0 = bx * TX, y0 = by * TY;
   int pw, pfx, pfy, pa, pr;
   fast_planes(RECON, TY, &pw, &pfx, &pfy, &pa, &pr);
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel_fast(const StagePa
   t.Rt = t.A + pa;
 
   const R* __restrict__ U = static_cast<const R*>(p.U);
-  if (tid == 0) s_sdt = static_cast<R>(p.beta * p.clock->dt);
+  if (tid == 0) *s_sdt = static_cast<R>(p.beta * p.clock->dt);
 
   const int PH = TY + 2 * H;
   for (int idx = tid; idx < PW * PH; idx += kStageThreads) {
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel_fast(const StagePa
   const R* __restrict__ V = static_cast<const R*>(p.V);
   R* Uo = static_cast<R*>(p.Uout);
   R* Vo = static_cast<R*>(p.Vout);
-  const R sdt = s_sdt;
+  const R sdt = *s_sdt;
   const R kdrag = sdt * k.drag;
   R vmax0 = R(0), vmax1 = R(0);
   for (int idx = tid; idx < TY * TX; idx += kStageThreads) {
@@ -347,11 +347,48 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel_fast(const StagePa
     double vmax[2] = {static_cast<double>(vmax0), static_cast<double>(vmax1)};
     block_nan_max<2>(vmax, red);
     if (tid == 0) {
-      p.partials[(size_t)blockIdx.x * kCflSlots + 0] = vmax[0];
-      p.partials[(size_t)blockIdx.x * kCflSlots + 1] = vmax[1];
-      p.partials[(size_t)blockIdx.x * kCflSlots + 2] = 0.0;
-      if (blockIdx.x == 0) p.header->n_cfl = gridDim.x;
+      p.partials[(size_t)tile * kCflSlots + 0] = vmax[0];
+      p.partials[(size_t)tile * kCflSlots + 1] = vmax[1];
+      p.partials[(size_t)tile * kCflSlots + 2] = 0.0;
+      if (tile == 0) p.header->n_cfl = ntiles;
     }
+  }
+}
+
+template <typename R, int RECON, int RS, int NV>
+__global__ void __launch_bounds__(kStageThreads) stage_kernel_fast(const StageParams p) {
+  if (p.clock->done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32 * 2];
+  __shared__ R s_sdt;
+  fast_tile<R, RECON, RS, NV>(p, blockIdx.x, gridDim.x, smem_raw, red, &s_sdt);
+}
+
+// Persistent stage kernel over many solves (one group: same precision,
+// reconstruction and Riemann solver; 3 or 4 variables per solve). Work item w
+// is tile w - tile_offset[i] of solve i. Blocks take work items round-robin;
+// a solve that is done, or whose integrator has fewer stages, is skipped.
+template <typename R, int RECON, int RS>
+__global__ void __launch_bounds__(kStageThreads) stage_kernel_batch(const StageParams* __restrict__ params,
+                                                                    const int* __restrict__ tile_offset,
+                                                                    int nsolves, int nwork) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32 * 2];
+  __shared__ R s_sdt;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    int lo = 0, hi = nsolves - 1;  // last solve whose offset <= w
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile_offset[mid] <= w) lo = mid;
+      else hi = mid - 1;
+    }
+    const StageParams& p = params[lo];
+    if (p.skip || p.clock->done) continue;
+    const int tile = w - tile_offset[lo];
+    const int ntiles = tile_offset[lo + 1] - tile_offset[lo];
+    __syncthreads();  // the previous tile's last readers of shared memory are done
+    if (p.nv == 3) fast_tile<R, RECON, RS, 3>(p, tile, ntiles, smem_raw, red, &s_sdt);
+    else fast_tile<R, RECON, RS, 4>(p, tile, ntiles, smem_raw, red, &s_sdt);
   }
 }
 
@@ -379,6 +416,58 @@ cudaError_t launch_fast_rs(int rsolver, const StageParams& p, dim3 grid, size_t 
     case JX_ROE: return launch_fast_one<R, RECON, JX_ROE, NV>(p, grid, smem, s);
   }
   return cudaErrorInvalidValue;
+}
+
+template <typename R, int RECON>
+cudaError_t launch_batch_rs(int rsolver, const StageParams* params, const int* offsets, int nsolves, int nwork,
+                            dim3 grid, size_t smem, cudaStream_t s) {
+  auto pick = [&](auto kernel) -> cudaError_t {
+    static int granted[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if ((int)smem > granted[dev]) {
+      cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      granted[dev] = (int)smem;
+    }
+    kernel<<<grid, kStageThreads, smem, s>>>(params, offsets, nsolves, nwork);
+    return cudaGetLastError();
+  };
+  switch (rsolver) {
+    case JX_LLF: return pick(stage_kernel_batch<R, RECON, JX_LLF>);
+    case JX_HLLE: return pick(stage_kernel_batch<R, RECON, JX_HLLE>);
+    case JX_ROE: return pick(stage_kernel_batch<R, RECON, JX_ROE>);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int RECON>
+cudaError_t launch_batch_recon(int dtype, int rsolver, const StageParams* params, const int* offsets, int nsolves,
+                               int nwork, dim3 grid, size_t smem, cudaStream_t s) {
+  if (dtype == JX_F64) return launch_batch_rs<double, RECON>(rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+  return launch_batch_rs<float, RECON>(rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+}
+
+// Blocks of the persistent batch kernel that fit on one SM.
+template <typename R, int RECON, int RS>
+int batch_blocks_per_sm_rs(size_t smem) {
+  int n = 0;
+  cudaFuncSetAttribute(stage_kernel_batch<R, RECON, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage_kernel_batch<R, RECON, RS>, kStageThreads, smem);
+  return n;
+}
+
+template <int RECON>
+int batch_blocks_per_sm_recon(int dtype, int rsolver, size_t smem) {
+  if (dtype == JX_F64) {
+    if (rsolver == JX_LLF) return batch_blocks_per_sm_rs<double, RECON, JX_LLF>(smem);
+    if (rsolver == JX_HLLE) return batch_blocks_per_sm_rs<double, RECON, JX_HLLE>(smem);
+    return batch_blocks_per_sm_rs<double, RECON, JX_ROE>(smem);
+  }
+  if (rsolver == JX_LLF) return batch_blocks_per_sm_rs<float, RECON, JX_LLF>(smem);
+  if (rsolver == JX_HLLE) return batch_blocks_per_sm_rs<float, RECON, JX_HLLE>(smem);
+  return batch_blocks_per_sm_rs<float, RECON, JX_ROE>(smem);
 }
 
 template <int RECON>

@@ -17,4 +17,11 @@ cudaError_t launch_fast_dc(int dtype, int rsolver, const StageParams& p, dim3 gr
                            cudaStream_t s) {
   return launch_fast_recon<JX_DC>(dtype, rsolver, p, grid, smem, s);
 }
+cudaError_t launch_batch_dc(int dtype, int rsolver, const StageParams* params, const int* offsets, int nsolves,
+                            int nwork, dim3 grid, size_t smem, cudaStream_t s) {
+  return launch_batch_recon<JX_DC>(dtype, rsolver, params, offsets, nsolves, nwork, grid, smem, s);
+}
+int batch_blocks_per_sm_dc(int dtype, int rsolver, size_t smem) {
+  return batch_blocks_per_sm_recon<JX_DC>(dtype, rsolver, smem);
+}
 }  // namespace jx

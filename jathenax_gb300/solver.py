@@ -22,7 +22,7 @@ class Solve:
     def __init__(self, U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *,
                  viscosity=0.0, smagorinsky_cs=0.0, drag_rate=0.0, forcing=None,
                  dt_update=1.0, tdriv_start=0.0, dedt=0.0, reconstruct="ppm4", rsolver="roe",
-                 predict_stress=None, sgs_weights=None, tile=(0, 0), dtype=None):
+                 predict_stress=None, sgs_weights=None, tile=(0, 0), dtype=None, clock=None):
         t = _lib.torch()
         RK_STAGES[integrator]
         self.U = _lib.to_device(U, dtype)
@@ -46,9 +46,16 @@ class Solve:
             raw = t.zeros(tuple(self.S.shape[:2]) + (2,), dtype=self.S.dtype, device=self.S.device)
             self.forcing = _Forcing(raw, tables)
             n_updates = tables[0].shape[0]
-        self.clock = _lib.new_clock(
+        fresh = _lib.new_clock(
             tlim=float(tlim), nlim=int(nlim), cfl=float(cfl), t_start=float(tdriv_start),
             dt_update=float(dt_update), dedt=float(dedt), n_updates=n_updates)
+        if clock is None:
+            self.clock = fresh
+        else:  # a 128-byte slice of a caller's buffer (batches read all clocks at once)
+            if clock.numel() != 128 or clock.dtype != t.uint8:
+                raise ValueError("clock storage must be 128 uint8 elements")
+            clock.copy_(fresh)
+            self.clock = clock
         self._idle_clock = _lib.new_clock(done=1)
         self.graph = None
         self.graph_steps = 0
@@ -98,6 +105,18 @@ class Solve:
     # -- driving --------------------------------------------------------------
     def state(self):
         return _lib.read_clock(self.clock)
+
+    def as_jx_solve(self):
+        """This solve as the C ABI's jx_solve (for batches)."""
+        js = _lib.SolveStruct()
+        js.desc = self.desc
+        js.S, js.A, js.B = self.S.data_ptr(), self.A.data_ptr(), self.B.data_ptr()
+        js.clock = self.clock.data_ptr()
+        if self.forcing is not None:
+            js.forcing = self.forcing.struct
+        js.workspace = self.ws.data_ptr()
+        js.workspace_bytes = self.nbytes
+        return js
 
     def run(self, steps_per_sync=32, use_graph=True):
         """Advance until tlim or nlim; returns the final clock."""

@@ -1,0 +1,81 @@
+"""Batches of uneven solves: each result is bitwise the same alone and in the mix."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_solve(kind, n, dtype, recon, rsolver, integrator, tlim, tile_y, clock=None, seed=1618):
+    import torch
+    from jathenax_gb300.forcing import cartesian_modes, forcing_basis, modal_coefficients
+    from jathenax_gb300.initial_conditions import (
+        cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest)
+    from jathenax_gb300.solver import Solve
+    tdtype = getattr(torch, dtype)
+    kw = dict(reconstruct=recon, rsolver=rsolver, tile=(32, tile_y), dtype=tdtype, clock=clock)
+    if kind == "kh":
+        U = kelvin_helmholtz_tanh(n, n)
+        return Solve(U, 1 / n, 1 / n, 1.0, 1e-10, integrator, 0.4, tlim, 10**6, **kw)
+    if kind == "smooth":
+        return Solve(smooth_waves(n, n + 8), 1 / n, 1 / (n + 8), 1.0, 1e-10, integrator, 0.4, tlim,
+                     10**6, **kw)
+    x, _ = cell_centers(n, n)
+    modes = cartesian_modes(3, 5, (-5, 5), (-5, 5))
+    updates = int(np.ceil(tlim / 0.0075)) + 1
+    table = modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, seed, 0.75, 0.0075, updates)
+    basis = forcing_basis(modes, x, x, (1.0, 1.0))
+    return Solve(uniform_rest(n, n), 1 / n, 1 / n, 1.0, 1.17549e-38, integrator, 0.4, tlim, 10**6,
+                 viscosity=1.5e-6, drag_rate=0.3333335, forcing=(table, basis), dt_update=0.0075,
+                 dedt=0.03703705, **kw)
+
+
+SPECS = [  # kind, n, dtype, recon, rsolver, integrator, tlim
+    ("kh", 64, "float32", "ppm4", "roe", "rk3", 0.05),
+    ("kh", 96, "float32", "ppm4", "roe", "rk3", 0.03),
+    ("turb", 48, "float32", "ppm4", "roe", "rk3", 0.06),
+    ("turb", 32, "float32", "ppm4", "roe", "rk3", 0.04),
+    ("smooth", 40, "float64", "wenoz", "hlle", "rk4", 0.02),
+    ("kh", 72, "float64", "ppmx", "llf", "rk2", 0.03),
+    ("smooth", 24, "float32", "plm", "roe", "rk3", 0.05),
+]
+
+
+def run_alone(spec, tile_y):
+    s = make_solve(*spec, tile_y=tile_y)
+    s.run(steps_per_sync=8)
+    c = s.state()
+    return s.S.cpu().numpy(), c.time, c.cycle
+
+
+@pytest.mark.parametrize("tile_y", [16])
+def test_batch_results_equal_solo_results_bitwise(tile_y):
+    from jathenax_gb300.batch import Batch, ClockBank
+    bank = ClockBank(len(SPECS))
+    solves = [make_solve(*spec, tile_y=tile_y, clock=bank.slot(i)) for i, spec in enumerate(SPECS)]
+    batch = Batch(solves, clocks=bank)
+    assert batch.groups == 4
+    clocks = batch.run(steps_per_sync=8)
+    for spec, s, c in zip(SPECS, solves, clocks):
+        U_alone, t_alone, cyc_alone = run_alone(spec, tile_y)
+        assert c.done and c.cycle == cyc_alone and c.time == t_alone, spec
+        np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=str(spec))
+
+
+def test_batch_tile_height_does_not_change_results():
+    from jathenax_gb300.batch import Batch
+    outs = []
+    for tile_y in (8, 32):
+        solves = [make_solve(*spec, tile_y=tile_y) for spec in SPECS[:4]]
+        Batch(solves, blocks_per_sm=2).run(steps_per_sync=4, use_graph=False)
+        outs.append([s.S.cpu().numpy() for s in solves])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_batch_rejects_mixed_tiles_and_wide_states():
+    from jathenax_gb300.batch import Batch
+    a = make_solve("kh", 32, "float32", "ppm4", "roe", "rk3", 0.01, tile_y=16)
+    b = make_solve("kh", 32, "float32", "ppm4", "roe", "rk3", 0.01, tile_y=8)
+    with pytest.raises(ValueError, match="share one"):
+        Batch([a, b])
