@@ -1,0 +1,99 @@
+"""Autotuner for the batched stage kernel.
+
+Searches the tile height (32 x 8, 16 or 32 cells: the shared-memory tile and
+its halo, 256 threads each) and the number of persistent blocks per SM
+(occupancy limit or 1..4) for one (precision, reconstruction, Riemann solver,
+variable count) kernel class on a probe grid, timing a few evolve cycles of
+each candidate with CUDA events. The tile height never changes results (each
+cell's arithmetic is the same and the CFL reduction is an exact maximum), so
+the choice is purely about speed. Choices are cached per GPU model in
+memory and in ``$JATHENAX_GB300_CACHE`` (default
+``~/.cache/jathenax_gb300/autotune.json``).
+"""
+
+import json
+import os
+from pathlib import Path
+
+from . import _lib
+
+TILE_HEIGHTS = (8, 16, 32)
+BLOCKS_PER_SM = (0, 1, 2, 3, 4)
+_memory = {}
+
+
+def _cache_path():
+    root = os.environ.get("JATHENAX_GB300_CACHE")
+    return Path(root) if root else Path.home() / ".cache" / "jathenax_gb300" / "autotune.json"
+
+
+def _load():
+    try:
+        return json.loads(_cache_path().read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key, value):
+    data = _load()
+    data[key] = value
+    try:
+        path = _cache_path()
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_text(json.dumps(data, indent=1, sort_keys=True))
+    except OSError:
+        pass
+
+
+def _probe_state(nvar, side):
+    from .initial_conditions import kelvin_helmholtz_tanh, smooth_waves
+    return kelvin_helmholtz_tanh(side, side) if nvar == 4 else smooth_waves(side, side)
+
+
+def measure(dtype, reconstruct, rsolver, nvar, side, tile_y, blocks_per_sm, steps=4):
+    """Milliseconds per evolve cycle of one probe solve run through the batch path."""
+    t = _lib.torch()
+    from .batch import Batch
+    from .solver import Solve
+    solve = Solve(_probe_state(nvar, side), 1.0 / side, 1.0 / side, 1.0, 1e-10, "rk3", 0.4, 1e30,
+                  2**31 - 1, reconstruct=reconstruct, rsolver=rsolver, tile=(32, tile_y),
+                  dtype=getattr(t, dtype))
+    batch = Batch([solve], blocks_per_sm=blocks_per_sm)
+    for _ in range(2):
+        batch.enqueue_step()
+    start, end = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        batch.enqueue_step()
+    end.record()
+    end.synchronize()
+    return start.elapsed_time(end) / steps
+
+
+def tune(dtype="float32", reconstruct="ppm4", rsolver="roe", nvar=4, side=1024, steps=4,
+         use_cache=True):
+    """Return {"tile_y": ..., "blocks_per_sm": ..., "ms_per_step": ..., "trials": [...]}."""
+    t = _lib.torch()
+    key = "|".join(map(str, (t.cuda.get_device_name(), dtype, reconstruct, rsolver, nvar, side)))
+    if use_cache:
+        if key in _memory:
+            return _memory[key]
+        stored = _load().get(key)
+        if stored:
+            _memory[key] = stored
+            return stored
+    trials = []
+    for tile_y in TILE_HEIGHTS:
+        for bps in BLOCKS_PER_SM:
+            try:
+                ms = measure(dtype, reconstruct, rsolver, nvar, side, tile_y, bps, steps)
+            except (ValueError, RuntimeError):  # tile does not fit in shared memory
+                continue
+            trials.append({"tile_y": tile_y, "blocks_per_sm": bps, "ms_per_step": ms})
+    if not trials:
+        raise RuntimeError("no autotuning candidate could run")
+    best = min(trials, key=lambda r: r["ms_per_step"])
+    result = dict(best, trials=trials, key=key)
+    _memory[key] = result
+    _store(key, result)
+    return result

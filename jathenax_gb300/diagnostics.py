@@ -1,0 +1,79 @@
+"""Diagnostics on host copies of states: spectra, errors, conservation drift.
+
+``shell_spectra`` restates the reference's analysis script
+(jathenax/spectra.py:22-41): density-weighted kinetic energy of sqrt(rho) v
+and the Fourier-curl enstrophy, summed over integer shells
+floor(|k| + 0.5), without plotting. The error helpers are the Precision
+pattern's metrics: relative L1 error per component, box-integrated drift of
+the conserved sums (run.py:186-187), and the kinetic-energy spectrum
+deviation.
+"""
+
+import numpy as np
+
+
+def shell_spectra(U):
+    """Return (modes, kinetic_energy, enstrophy) per integer shell (spectra.py:22-41)."""
+    U = np.asarray(U, dtype=np.float64)
+    rho, mx, my = np.moveaxis(U[..., :3], -1, 0)
+    ny, nx = rho.shape
+    kx, ky = np.fft.fftfreq(nx) * nx, np.fft.fftfreq(ny) * ny
+    radius = np.hypot(kx[None, :], ky[:, None])
+    shell = np.floor(radius + 0.5).astype(int)
+    modes = np.arange(shell.max() + 1)
+    vx, vy = mx / rho, my / rho
+    root = np.sqrt(rho)
+    ax = np.fft.fft2(root * vx) / rho.size
+    ay = np.fft.fft2(root * vy) / rho.size
+    energy = np.bincount(shell.ravel(), (0.5 * (np.abs(ax)**2 + np.abs(ay)**2)).ravel(),
+                         minlength=len(modes))
+    # The axis Nyquist mode has no real derivative.
+    kxd, kyd = kx.copy(), ky.copy()
+    if nx % 2 == 0:
+        kxd[nx // 2] = 0
+    if ny % 2 == 0:
+        kyd[ny // 2] = 0
+    omega = 2j * np.pi * (kxd[None, :] * np.fft.fft2(vy) - kyd[:, None] * np.fft.fft2(vx))
+    enstrophy = np.bincount(shell.ravel(), (0.5 * np.abs(omega / rho.size)**2).ravel(),
+                            minlength=len(modes))
+    return modes, energy, enstrophy
+
+
+def relative_l1(a, b):
+    """Per component: mean |a - b| / mean |b| over the grid (float64)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    num = np.mean(np.abs(a - b), axis=(0, 1))
+    den = np.maximum(np.mean(np.abs(b), axis=(0, 1)), 1e-300)
+    return num / den
+
+
+def box_drift(U, U0, dx, dy):
+    """Change of the box-integrated conserved quantities (run.py:186-187)."""
+    return (np.asarray(U).sum(axis=(0, 1), dtype=np.float64)
+            - np.asarray(U0).sum(axis=(0, 1), dtype=np.float64)) * dx * dy
+
+
+def spectrum_deviation(U, U_ref, shells=None):
+    """Largest relative deviation of the KE shell spectrum over shells 1..min(nx, ny)//2 - 1."""
+    _, e, _ = shell_spectra(U)
+    _, e_ref, _ = shell_spectra(U_ref)
+    ny, nx = np.shape(U)[:2]
+    hi = shells if shells is not None else max(2, min(nx, ny) // 2)
+    sl = slice(1, hi)
+    ref = np.maximum(e_ref[sl], 1e-300)
+    return float(np.max(np.abs(e[sl] - e_ref[sl]) / ref))
+
+
+def precision_report(U32, U64, U0, dx, dy):
+    """The FP32-vs-FP64 error record used by the Precision pattern."""
+    l1 = relative_l1(U32, U64)
+    drift32 = box_drift(U32, U0, dx, dy)
+    drift64 = box_drift(U64, U0, dx, dy)
+    return {
+        "l1_density": float(l1[0]),
+        "l1_momentum": float(max(l1[1], l1[2])),
+        "drift_fp32": [float(v) for v in drift32[:3]],
+        "drift_fp64": [float(v) for v in drift64[:3]],
+        "ke_spectrum_max_rel_dev": spectrum_deviation(U32, U64),
+    }

@@ -1,0 +1,200 @@
+"""Serving: a continuously batched request loop over device-resident solves.
+
+Requests (problem, grid side, reconstruction, Riemann solver, end time,
+precision, seed) arrive over time. A request is admitted when it has arrived
+and its device memory (three states, workspace, forcing tables) fits in the
+HBM budget next to the live solves; it then stays resident on the GPU until
+it reaches its end time. Every tick advances all live solves together through
+one :class:`jathenax_gb300.batch.Batch` step per cycle; between ticks
+finished solves leave (their memory returns to the budget) and waiting
+requests join, so new work overlaps with solves already on the device.
+Because batches are exact (a solve's result does not depend on its
+neighbours), each result equals the result of running that request alone.
+
+The reported metrics are time-to-solution (completion minus arrival:
+queueing + compute) percentiles and solves per second.
+"""
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+PROBLEMS = ("smooth", "kh", "turbulence")
+RECONS = ("dc", "plm", "ppm4", "ppmx", "wenoz")
+SOLVERS = ("llf", "hlle", "roe")
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float        # seconds after the stream starts
+    problem: str
+    side: int
+    reconstruct: str
+    rsolver: str
+    tlim: float
+    dtype: str            # "float32" or "float64"
+    seed: int
+    admitted: float = None
+    finished: float = None
+    cycles: int = 0
+    result: object = field(default=None, repr=False)
+
+
+def make_stream(n, rate, seed=0, side_range=(64, 2048), tlim_range=(0.2, 3.0), fp32_fraction=0.8,
+                problems=PROBLEMS, recons=RECONS, solvers=SOLVERS):
+    """Poisson arrivals at `rate` per second; side log-uniform; tlim uniform."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    lo, hi = np.log(side_range[0]), np.log(side_range[1])
+    out = []
+    for i in range(n):
+        side = int(round(float(np.exp(rng.uniform(lo, hi)))))
+        out.append(Request(
+            rid=i, arrival=float(arrivals[i]), problem=str(rng.choice(problems)), side=max(side, 6),
+            reconstruct=str(rng.choice(recons)), rsolver=str(rng.choice(solvers)),
+            tlim=float(rng.uniform(*tlim_range)),
+            dtype="float32" if rng.random() < fp32_fraction else "float64",
+            seed=int(rng.integers(1, 2**31 - 1))))
+    return out
+
+
+def build_solve(req, tile_y=16, clock=None, dtype=None):
+    """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163)."""
+    t = _lib.torch()
+    from .forcing import cartesian_modes, forcing_basis, modal_coefficients
+    from .initial_conditions import cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest
+    from .solver import Solve
+    n = req.side
+    kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver, tile=(32, tile_y),
+              dtype=getattr(t, dtype or req.dtype), clock=clock)
+    if req.problem == "kh":
+        return Solve(kelvin_helmholtz_tanh(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
+    if req.problem == "smooth":
+        return Solve(smooth_waves(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
+    x, _ = cell_centers(n, n)
+    modes = cartesian_modes(3, 5, (-5, 5), (-5, 5))
+    updates = int(np.ceil(req.tlim / 0.0075)) + 1
+    table = modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, req.seed, 0.75, 0.0075, updates)
+    basis = forcing_basis(modes, x, x, (1.0, 1.0))
+    return Solve(uniform_rest(n, n), 1 / n, 1 / n, 1.0, 1.17549e-38, "rk3", 0.4, req.tlim, 10**7,
+                 viscosity=1.5e-6, drag_rate=0.3333335, forcing=(table, basis), dt_update=0.0075,
+                 dedt=0.03703705, **kw)
+
+
+def footprint_bytes(req):
+    """Device bytes a request holds while live (states, workspace, forcing tables)."""
+    nvar = 4 if req.problem == "kh" else 3
+    w = 4 if req.dtype == "float32" else 8
+    cells = req.side * req.side
+    states = 3 * cells * nvar * w
+    workspace = (cells // (32 * 8) + 4096) * 32 + 64 * 1024
+    forcing = 0
+    if req.problem == "turbulence":
+        updates = int(np.ceil(req.tlim / 0.0075)) + 1
+        forcing = updates * 56 * 32 + 4 * 56 * req.side * w + cells * 2 * w
+    return states + workspace + forcing
+
+
+class Server:
+    """Continuous-batching request loop with an HBM admission budget."""
+
+    def __init__(self, budget_bytes=150e9, tile_y=16, steps_per_tick=4, blocks_per_sm=0,
+                 max_live=1024, keep_results=False):
+        self.budget = float(budget_bytes)
+        self.tile_y = tile_y
+        self.steps_per_tick = steps_per_tick
+        self.blocks_per_sm = blocks_per_sm
+        self.max_live = max_live
+        self.keep_results = keep_results
+
+    def run(self, requests):
+        """Serve `requests` (arrival-ordered or not); returns a stats dict."""
+        t = _lib.torch()
+        from .batch import Batch, ClockBank
+        bank = ClockBank(self.max_live)
+        free_slots = list(range(self.max_live - 1, -1, -1))
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        live = []          # (req, solve, slot)
+        in_use = 0.0
+        batch = None
+        changed = True
+        ticks = 0
+        peak_live = 0
+        peak_bytes = 0.0
+        t.cuda.synchronize()
+        t0 = time.perf_counter()
+        while pending or live:
+            now = time.perf_counter() - t0
+            while (pending and pending[0].arrival <= now and free_slots
+                   and in_use + footprint_bytes(pending[0]) <= self.budget):
+                req = pending.popleft()
+                slot = free_slots.pop()
+                solve = build_solve(req, self.tile_y, clock=bank.slot(slot))
+                req.admitted = time.perf_counter() - t0
+                live.append((req, solve, slot))
+                in_use += footprint_bytes(req)
+                peak_bytes = max(peak_bytes, in_use)
+                changed = True
+            if not live:
+                if pending:
+                    wait = pending[0].arrival - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(min(wait, 0.01))
+                    elif in_use + footprint_bytes(pending[0]) > self.budget:
+                        raise RuntimeError(f"request {pending[0].rid} does not fit in the HBM budget")
+                continue
+            if changed:
+                batch = Batch([s for _, s, _ in live], blocks_per_sm=self.blocks_per_sm)
+                changed = False
+            for _ in range(self.steps_per_tick):
+                batch.enqueue_step()
+            ticks += 1
+            peak_live = max(peak_live, len(live))
+            clocks = bank.read()  # one device-to-host copy of every clock (synchronises)
+            stamp = time.perf_counter() - t0
+            still = []
+            for req, solve, slot in live:
+                c = clocks[slot]
+                if c.done:
+                    if not (c.time == c.tlim or c.cycle >= c.nlim) or not np.isfinite(c.time):
+                        raise RuntimeError(f"request {req.rid} ended at t={c.time} after {c.cycle} steps")
+                    req.finished = stamp
+                    req.cycles = c.cycle
+                    if self.keep_results:
+                        req.result = solve.S.cpu().numpy()
+                    free_slots.append(slot)
+                    in_use -= footprint_bytes(req)
+                    changed = True
+                else:
+                    still.append((req, solve, slot))
+            live = still
+        elapsed = time.perf_counter() - t0
+        tts = np.array([r.finished - r.arrival for r in requests])
+        return {
+            "requests": len(requests), "elapsed_s": elapsed,
+            "solves_per_s": len(requests) / elapsed,
+            "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
+            "ticks": ticks, "peak_live": peak_live, "peak_bytes": peak_bytes,
+        }
+
+
+def run_serial(requests, dtype="float64", keep_results=False):
+    """The baseline: each request alone, one after another, in `dtype`."""
+    t = _lib.torch()
+    t.cuda.synchronize()
+    t0 = time.perf_counter()
+    for req in requests:
+        solve = build_solve(req, dtype=dtype)
+        solve.run(steps_per_sync=32)
+        if keep_results:
+            req.result = solve.S.cpu().numpy()
+        del solve
+    t.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    return {"requests": len(requests), "elapsed_s": elapsed, "solves_per_s": len(requests) / elapsed}

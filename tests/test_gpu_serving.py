@@ -1,0 +1,38 @@
+"""Serving: continuous batching admits requests by HBM budget; every result
+equals the same request run alone, bitwise."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_stream(n=10, seed=3, rate=400.0):
+    from jathenax_gb300.serve import make_stream
+    return make_stream(n, rate, seed=seed, side_range=(24, 96), tlim_range=(0.005, 0.03),
+                       fp32_fraction=0.6)
+
+
+def test_each_served_result_equals_the_request_run_alone():
+    from jathenax_gb300.serve import Server, build_solve
+    reqs = small_stream()
+    assert len({r.problem for r in reqs}) >= 2 and len({r.dtype for r in reqs}) == 2
+    stats = Server(budget_bytes=1e9, steps_per_tick=3, keep_results=True).run(reqs)
+    assert stats["requests"] == len(reqs) and stats["peak_live"] >= 2
+    assert 0 < stats["tts_p50_s"] <= stats["tts_p99_s"]
+    for r in reqs:
+        alone = build_solve(r)
+        alone.run(steps_per_sync=4)
+        np.testing.assert_array_equal(r.result, alone.S.cpu().numpy(), err_msg=str(r))
+        assert r.cycles == alone.state().cycle
+
+
+def test_admission_holds_live_memory_under_the_budget():
+    from jathenax_gb300.serve import Server, footprint_bytes
+    reqs = small_stream(8, seed=5)
+    budget = 2.2 * max(footprint_bytes(r) for r in reqs)
+    stats = Server(budget_bytes=budget, steps_per_tick=2).run(reqs)
+    assert stats["requests"] == 8
+    assert 0 < stats["peak_bytes"] <= budget
+    assert stats["peak_live"] < 8
+    assert all(r.finished >= r.admitted >= r.arrival for r in reqs)
