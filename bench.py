@@ -39,7 +39,7 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # ncu-measured DRAM bytes per cell for one launch of the fused stage kernel
 # (stage 2 of RK3, ppm4+roe, 4 variables), from the capture summarised in
 # profiles/; None until such a capture exists for the dtype.
-STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": None, "f32": None}
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": 377.4e6 / 2048**2, "f32": 175.1e6 / 2048**2}
 
 
 def parse_args():
@@ -53,6 +53,9 @@ def parse_args():
     p.add_argument("--only-fp32", action="store_true", help="time only the float32 state (profiling)")
     p.add_argument("--cpu-sample", type=int, default=512, help="grid side of the CPU sample")
     p.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU sample")
+    p.add_argument("--no-patterns", action="store_true",
+                   help="skip the batched / serving / precision measurements")
+    p.add_argument("--serve-requests", type=int, default=100)
     return p.parse_args()
 
 
@@ -328,7 +331,109 @@ def bench_ours(args, world, rank, local):
         line["gpu_launches"] += 4 * args.steps
     if rank == 0 and world == 1 and args.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
+    if rank == 0 and world == 1 and not args.no_patterns:
+        line["batched"] = bench_batched(torch)
+        line["serving"] = bench_serving(torch, args.serve_requests)
+        line["precision"] = bench_precision(torch)
     return line
+
+
+# ---------------------------------------------------------------------------
+# The three added patterns, each against the plain float64 path.
+# ---------------------------------------------------------------------------
+def ensemble_specs():
+    """64 solves: 16 each of 128^2..1024^2, alternating KH (4 vars) and driven turbulence (3 vars)."""
+    specs = []
+    seed = 1
+    for side in (128, 256, 512, 1024):
+        for i in range(16):
+            if i % 2 == 0:
+                specs.append(("kh", side, None))
+            else:
+                specs.append(("turbulence", side, seed))
+                seed += 1
+    return specs
+
+
+def make_request(kind, side, seed, tlim, dtype, rid=0):
+    from jathenax_gb300.serve import Request
+    return Request(rid=rid, arrival=0.0, problem=kind, side=side, reconstruct="ppm4", rsolver="roe",
+                   tlim=tlim, dtype=dtype, seed=seed or 1)
+
+
+def bench_batched(torch, tlim=0.02):
+    """Batched ensemble (float32, one persistent launch per stage, graph-captured)
+    against looping the plain float64 kernel over the same 64 solves."""
+    from jathenax_gb300 import autotune
+    from jathenax_gb300.batch import Batch, ClockBank
+    from jathenax_gb300.diagnostics import relative_l1
+    from jathenax_gb300.serve import build_solve
+    reqs = [make_request(k, n, s, tlim, "float32", i) for i, (k, n, s) in enumerate(ensemble_specs())]
+    tuned = autotune.tune("float32", "ppm4", "roe", 4, 1024)
+    bank = ClockBank(len(reqs))
+    solves = [build_solve(r, tuned["tile_y"], clock=bank.slot(i)) for i, r in enumerate(reqs)]
+    batch = Batch(solves, blocks_per_sm=tuned["blocks_per_sm"], clocks=bank)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.run(steps_per_sync=16)
+    torch.cuda.synchronize()
+    batched_s = time.perf_counter() - t0
+    out32 = [s.S.cpu().numpy() for s in solves]
+    del batch, solves
+    t0 = time.perf_counter()
+    l1 = []
+    for r, u32 in zip(reqs, out32):
+        s64 = build_solve(r, dtype="float64")
+        s64.run(steps_per_sync=32)
+        l1.append(float(relative_l1(u32, s64.S.cpu().numpy())[0]))
+        del s64
+    torch.cuda.synchronize()
+    serial_s = time.perf_counter() - t0
+    return {"solves": len(reqs), "workload": "16 each of 128^2/256^2/512^2/1024^2, KH (4 vars) and "
+            f"driven turbulence (3 vars, seeds 1..32), ppm4+roe rk3, tlim {tlim}",
+            "batched_fp32_solves_per_s": round(len(reqs) / batched_s, 3),
+            "serial_fp64_solves_per_s": round(len(reqs) / serial_s, 3),
+            "speedup": round(serial_s / batched_s, 2),
+            "max_l1_density_err_fp32_vs_fp64": max(l1),
+            "tile_y": tuned["tile_y"], "blocks_per_sm": tuned["blocks_per_sm"],
+            "batched_s": round(batched_s, 3), "serial_s": round(serial_s, 3)}
+
+
+def bench_serving(torch, n):
+    """Scaled serving stream: Poisson arrivals, side log-uniform 64..512, tlim U[0.02, 0.2],
+    80% float32; continuous batching vs serial plain float64."""
+    from jathenax_gb300.diagnostics import relative_l1
+    from jathenax_gb300.serve import Server, make_stream, run_serial
+    reqs = make_stream(n, rate=200.0, seed=2026, side_range=(64, 512), tlim_range=(0.02, 0.2))
+    stats = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True).run(reqs)
+    served = {r.rid: r.result for r in reqs}
+    ref = make_stream(n, rate=200.0, seed=2026, side_range=(64, 512), tlim_range=(0.02, 0.2))
+    serial = run_serial(ref, dtype="float64", keep_results=True)
+    errs = [float(relative_l1(served[r.rid], r.result)[0]) for r, q in zip(ref, reqs) if q.dtype == "float32"]
+    return {"requests": n, "stream": "Poisson 200/s, side log-uniform 64..512, tlim U[0.02,0.2], problems "
+            "smooth/kh/turbulence, random recon/rsolver, 80% float32, 150 GB budget",
+            "solves_per_s": round(stats["solves_per_s"], 3), "tts_p50_s": round(stats["tts_p50_s"], 4),
+            "tts_p99_s": round(stats["tts_p99_s"], 4), "peak_live": stats["peak_live"],
+            "serial_fp64_solves_per_s": round(serial["solves_per_s"], 3),
+            "speedup": round(stats["solves_per_s"] / serial["solves_per_s"], 2),
+            "fp32_l1_density_err_vs_fp64_max": max(errs) if errs else None,
+            "fp32_l1_density_err_vs_fp64_median": float(np.median(errs)) if errs else None}
+
+
+def bench_precision(torch):
+    """FP32 state against the FP64 run of the same problem at the same end time."""
+    from jathenax_gb300.diagnostics import precision_report
+    from jathenax_gb300.serve import build_solve
+    out = {}
+    for kind, side, tlim in (("kh", 512, 0.05), ("turbulence", 256, 0.1)):
+        res = {}
+        for dtype in ("float32", "float64"):
+            s = build_solve(make_request(kind, side, 1618, tlim, dtype), dtype=dtype)
+            U0 = s.S.cpu().numpy().astype(np.float64)
+            s.run(steps_per_sync=32)
+            res[dtype] = s.S.cpu().numpy()
+        out[f"{kind}_{side}_t{tlim}"] = precision_report(res["float32"], res["float64"], U0, 1 / side, 1 / side)
+    return out
 
 
 def bench_reference(args, world, rank):
