@@ -244,6 +244,14 @@ jx_status jx_box_sums(const jx_desc* d, const void* U, double* out, void* worksp
 /* Tile shape and shared memory the stage kernel will use for `d`. */
 jx_status jx_tile_info(const jx_desc* d, int32_t* tile_x, int32_t* tile_y, int64_t* smem_bytes);
 
+/* modal_coefficients (forcing.py:63-100) on the host: the OU table
+ * [updates][n_modes][2 dir][2 re/im] for the seed, bit-identical to the
+ * reference's Python generator. modes: n_modes x 2 integers (kx, ky).
+ * Returns 0, or -1 for null/negative arguments. Host memory only. */
+int32_t jx_ou_table(const int32_t* modes, int32_t n_modes, double Lx, double Ly, int32_t nlow,
+                    int32_t nhigh, double npeak, double sol_fraction, int64_t seed, double tcorr,
+                    double dt_update, int32_t updates, double* out);
+
 /* Peak probe: `blocks` x 256 threads each run 8 independent chains of
  * `iters` dependent FMAs in the given dtype (2*8*iters flops per thread).
  * Timed by the caller with events to measure the FP64/FP32 pipe rate.

@@ -99,6 +99,7 @@ PROTOTYPES = {
     "jx_batch_plan": [ctypes.POINTER(SolveStruct), _I32, _I32, _P, _SZ],
     "jx_batch_step": [_P, _P, _I32, _P],
     "jx_batch_groups": [_P],
+    "jx_ou_table": [_P, _I32, _D, _D, _I32, _I32, _D, _D, _I64, _D, _D, _I32, _P],
 }
 _RESTYPES = {"jx_last_error": ctypes.c_char_p, "jx_version": ctypes.c_char_p,
              "jx_num_stages": ctypes.c_int32, "jx_batch_groups": ctypes.c_int32}

@@ -36,7 +36,7 @@ class Batch:
     and have 3 or 4 variables.
     """
 
-    def __init__(self, solves, blocks_per_sm=0, clocks=None):
+    def __init__(self, solves, blocks_per_sm=0, clocks=None, plan_buffers=None):
         t = _lib.torch()
         self.solves = list(solves)
         if not self.solves:
@@ -51,9 +51,17 @@ class Batch:
         arr = (_lib.SolveStruct * n)(*[s.as_jx_solve() for s in self.solves])
         size = ctypes.c_size_t()
         _lib.call("jx_batch_plan_bytes", arr, n, self.tile_y, ctypes.byref(size))
-        self.plan_host = t.empty(int(size.value), dtype=t.uint8).pin_memory()
-        _lib.call("jx_batch_plan", arr, n, self.tile_y, ctypes.c_void_p(self.plan_host.data_ptr()), size.value)
-        self.plan_dev = self.plan_host.to(_lib.device(), non_blocking=False)
+        nbytes = int(size.value)
+        if plan_buffers is not None and plan_buffers[0].numel() >= nbytes:
+            # Reused (host pinned, device) pair, e.g. a server re-planning every tick.
+            self.plan_host, self.plan_dev = plan_buffers[0][:nbytes], plan_buffers[1][:nbytes]
+        else:
+            self.plan_host = t.empty(nbytes, dtype=t.uint8).pin_memory()
+            self.plan_dev = t.empty(nbytes, dtype=t.uint8, device=_lib.device())
+        _lib.call("jx_batch_plan", arr, n, self.tile_y, ctypes.c_void_p(self.plan_host.data_ptr()), nbytes)
+        # Stream-ordered copy: earlier steps that read an older plan in the same
+        # buffer are enqueued before it.
+        self.plan_dev.copy_(self.plan_host, non_blocking=True)
         self.groups = _lib.load().jx_batch_groups(ctypes.c_void_p(self.plan_host.data_ptr()))
         self.graph = None
 

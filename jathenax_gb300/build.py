@@ -36,15 +36,29 @@ def _compile(nvcc, source, flags):
     return obj, result.stderr
 
 
+def _compile_host(source):
+    """Host C++ (no device code), without FMA contraction so results match Python."""
+    obj = OBJDIR / (source.stem + ".o")
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    cmd = [cxx, "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-c", str(source), "-o", str(obj)]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"{cxx} failed on {source.name}:\n{result.stdout}\n{result.stderr}")
+    return obj, result.stderr
+
+
 def build(verbose=False, ptxas_info=False, jobs=None):
     """Compile every kernel for sm_103a and link libjx.so; returns its path."""
     nvcc = nvcc_path()
     OBJDIR.mkdir(exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
+    host_sources = sorted(CSRC.glob("*.cpp"))
     flags = ["-Xptxas", "-v"] if ptxas_info else []
-    jobs = jobs or min(len(sources), os.cpu_count() or 4)
+    jobs = jobs or min(len(sources) + len(host_sources), os.cpu_count() or 4)
     with ThreadPoolExecutor(max_workers=jobs) as pool:
-        results = list(pool.map(lambda s: _compile(nvcc, s, flags), sources))
+        futures = [pool.submit(_compile, nvcc, s, flags) for s in sources]
+        futures += [pool.submit(_compile_host, s) for s in host_sources]
+        results = [f.result() for f in futures]
     objects = [obj for obj, _ in results]
     if verbose or ptxas_info:
         for _, log in results:

@@ -89,7 +89,29 @@ def _fused_multiply_add(a, b, c):
 
 def modal_coefficients(modes, lengths, nlow, nhigh, npeak, sol_fraction, rseed,
                        tcorr, dt_update, updates):
-    """OU modal table [update, mode, dir, re/im] in float64 (forcing.py:63-100)."""
+    """OU modal table [update, mode, dir, re/im] in float64 (forcing.py:63-100).
+
+    Generated by libjx.so's host routine jx_ou_table, which is bit-identical
+    to :func:`modal_coefficients_python` and much faster for long runs.
+    """
+    if not nlow <= npeak <= nhigh or not 0.0 <= sol_fraction <= 1.0:
+        raise ValueError("npeak must be in the forcing band and sol_fraction in [0, 1]")
+    if not np.isfinite(tcorr) or tcorr < 0.0 or not 0.0 < dt_update < np.inf:
+        raise ValueError("tcorr must be finite and nonnegative and dt_update positive")
+    modes32 = np.ascontiguousarray(np.asarray(modes), dtype=np.int32)
+    out = np.empty((int(updates), len(modes32), 2, 2))
+    status = _lib.load().jx_ou_table(
+        modes32.ctypes.data_as(ctypes.c_void_p), len(modes32), float(lengths[0]), float(lengths[1]),
+        int(nlow), int(nhigh), float(npeak), float(sol_fraction), int(rseed), float(tcorr),
+        float(dt_update), int(updates), out.ctypes.data_as(ctypes.c_void_p))
+    if status != 0:
+        raise ValueError("invalid forcing table arguments")
+    return out
+
+
+def modal_coefficients_python(modes, lengths, nlow, nhigh, npeak, sol_fraction, rseed,
+                              tcorr, dt_update, updates):
+    """Pure-Python OU table, the step-by-step restatement of forcing.py:63-100."""
     if not nlow <= npeak <= nhigh or not 0.0 <= sol_fraction <= 1.0:
         raise ValueError("npeak must be in the forcing band and sol_fraction in [0, 1]")
     if not np.isfinite(tcorr) or tcorr < 0.0 or not 0.0 < dt_update < np.inf:

@@ -87,10 +87,10 @@ def build_solve(req, tile_y=16, clock=None, dtype=None):
                  dedt=0.03703705, **kw)
 
 
-def footprint_bytes(req):
+def footprint_bytes(req, dtype=None):
     """Device bytes a request holds while live (states, workspace, forcing tables)."""
     nvar = 4 if req.problem == "kh" else 3
-    w = 4 if req.dtype == "float32" else 8
+    w = 4 if (dtype or req.dtype) == "float32" else 8
     cells = req.side * req.side
     states = 3 * cells * nvar * w
     workspace = (cells // (32 * 8) + 4096) * 32 + 64 * 1024
@@ -105,19 +105,24 @@ class Server:
     """Continuous-batching request loop with an HBM admission budget."""
 
     def __init__(self, budget_bytes=150e9, tile_y=16, steps_per_tick=4, blocks_per_sm=0,
-                 max_live=1024, keep_results=False):
+                 max_live=1024, keep_results=False, dtype=None):
         self.budget = float(budget_bytes)
         self.tile_y = tile_y
         self.steps_per_tick = steps_per_tick
         self.blocks_per_sm = blocks_per_sm
         self.max_live = max_live
         self.keep_results = keep_results
+        self.dtype = dtype  # serve every request in this precision (None: as requested)
 
     def run(self, requests):
         """Serve `requests` (arrival-ordered or not); returns a stats dict."""
         t = _lib.torch()
         from .batch import Batch, ClockBank
         bank = ClockBank(self.max_live)
+        # One pinned/device pair for every re-plan (a plan is ~2.7 KB per solve).
+        plan_cap = 4096 + self.max_live * 4096
+        plan_bufs = (t.empty(plan_cap, dtype=t.uint8).pin_memory(),
+                     t.empty(plan_cap, dtype=t.uint8, device=_lib.device()))
         free_slots = list(range(self.max_live - 1, -1, -1))
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         live = []          # (req, solve, slot)
@@ -132,13 +137,13 @@ class Server:
         while pending or live:
             now = time.perf_counter() - t0
             while (pending and pending[0].arrival <= now and free_slots
-                   and in_use + footprint_bytes(pending[0]) <= self.budget):
+                   and in_use + footprint_bytes(pending[0], self.dtype) <= self.budget):
                 req = pending.popleft()
                 slot = free_slots.pop()
-                solve = build_solve(req, self.tile_y, clock=bank.slot(slot))
+                solve = build_solve(req, self.tile_y, clock=bank.slot(slot), dtype=self.dtype)
                 req.admitted = time.perf_counter() - t0
                 live.append((req, solve, slot))
-                in_use += footprint_bytes(req)
+                in_use += footprint_bytes(req, self.dtype)
                 peak_bytes = max(peak_bytes, in_use)
                 changed = True
             if not live:
@@ -146,11 +151,11 @@ class Server:
                     wait = pending[0].arrival - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(min(wait, 0.01))
-                    elif in_use + footprint_bytes(pending[0]) > self.budget:
+                    elif in_use + footprint_bytes(pending[0], self.dtype) > self.budget:
                         raise RuntimeError(f"request {pending[0].rid} does not fit in the HBM budget")
                 continue
             if changed:
-                batch = Batch([s for _, s, _ in live], blocks_per_sm=self.blocks_per_sm)
+                batch = Batch([s for _, s, _ in live], blocks_per_sm=self.blocks_per_sm, plan_buffers=plan_bufs)
                 changed = False
             for _ in range(self.steps_per_tick):
                 batch.enqueue_step()
@@ -169,7 +174,7 @@ class Server:
                     if self.keep_results:
                         req.result = solve.S.cpu().numpy()
                     free_slots.append(slot)
-                    in_use -= footprint_bytes(req)
+                    in_use -= footprint_bytes(req, self.dtype)
                     changed = True
                 else:
                     still.append((req, solve, slot))

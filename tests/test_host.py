@@ -144,3 +144,18 @@ def test_no_oracle_import_in_package():
     for path in package.rglob("*.py"):
         text = path.read_text()
         assert "import oracle" not in text and "from oracle" not in text, path
+
+
+@pytest.mark.parametrize("args", [
+    ((1.0, 1.0), 3, 5, 4.0, 1.0, 1618, 0.75, 0.0075, 40),
+    ((1.0, 2.0), 2, 4, 3.0, 0.3, 7, 0.5, 0.01, 12),
+    ((2.0, 1.0), 1, 3, 2.5, 0.0, 2**31 - 5, 0.0, 0.02, 9),
+])
+def test_native_ou_table_is_bitwise_the_python_generator(args):
+    lengths, nlow, nhigh = args[0], args[1], args[2]
+    modes = G.cartesian_modes(nlow, nhigh, (-nhigh, nhigh), (-nhigh, nhigh))
+    native = G.modal_coefficients(modes, *args)
+    python = G.modal_coefficients_python(modes, *args)
+    oracle = F.ou_table(modes, *args)
+    np.testing.assert_array_equal(native.view(np.uint64), python.view(np.uint64))
+    np.testing.assert_array_equal(native.view(np.uint64), oracle.view(np.uint64))
