@@ -42,6 +42,7 @@ class Request:
     admitted: float = None
     finished: float = None
     cycles: int = 0
+    error: str = None
     result: object = field(default=None, repr=False)
 
 
@@ -105,7 +106,7 @@ class Server:
     """Continuous-batching request loop with an HBM admission budget."""
 
     def __init__(self, budget_bytes=150e9, tile_y=16, steps_per_tick=4, blocks_per_sm=0,
-                 max_live=1024, keep_results=False, dtype=None):
+                 max_live=1024, keep_results=False, dtype=None, builder=None):
         self.budget = float(budget_bytes)
         self.tile_y = tile_y
         self.steps_per_tick = steps_per_tick
@@ -113,6 +114,7 @@ class Server:
         self.max_live = max_live
         self.keep_results = keep_results
         self.dtype = dtype  # serve every request in this precision (None: as requested)
+        self.builder = builder or build_solve  # (request, tile_y, clock, dtype) -> Solve
 
     def run(self, requests):
         """Serve `requests` (arrival-ordered or not); returns a stats dict."""
@@ -140,7 +142,7 @@ class Server:
                    and in_use + footprint_bytes(pending[0], self.dtype) <= self.budget):
                 req = pending.popleft()
                 slot = free_slots.pop()
-                solve = build_solve(req, self.tile_y, clock=bank.slot(slot), dtype=self.dtype)
+                solve = self.builder(req, self.tile_y, clock=bank.slot(slot), dtype=self.dtype)
                 req.admitted = time.perf_counter() - t0
                 live.append((req, solve, slot))
                 in_use += footprint_bytes(req, self.dtype)
@@ -167,11 +169,16 @@ class Server:
             for req, solve, slot in live:
                 c = clocks[slot]
                 if c.done:
-                    if not (c.time == c.tlim or c.cycle >= c.nlim) or not np.isfinite(c.time):
-                        raise RuntimeError(f"request {req.rid} ended at t={c.time} after {c.cycle} steps")
                     req.finished = stamp
                     req.cycles = c.cycle
-                    if self.keep_results:
+                    # A non-finite state drives dt to NaN and stops the solve
+                    # early (run.py:178-180 raises there); a tracer-only NaN
+                    # leaves dt finite, so the box sums are checked as well.
+                    sums = solve.box_sums()
+                    if not (c.time == c.tlim or c.cycle >= c.nlim) or not np.isfinite(c.time) \
+                            or not np.all(np.isfinite(sums)):
+                        req.error = f"stopped at t={c.time} after {c.cycle} steps (non-finite state)"
+                    elif self.keep_results:
                         req.result = solve.S.cpu().numpy()
                     free_slots.append(slot)
                     in_use -= footprint_bytes(req, self.dtype)
@@ -180,10 +187,11 @@ class Server:
                     still.append((req, solve, slot))
             live = still
         elapsed = time.perf_counter() - t0
-        tts = np.array([r.finished - r.arrival for r in requests])
+        ok = [r for r in requests if r.error is None]
+        tts = np.array([r.finished - r.arrival for r in ok]) if ok else np.array([np.nan])
         return {
-            "requests": len(requests), "elapsed_s": elapsed,
-            "solves_per_s": len(requests) / elapsed,
+            "requests": len(requests), "completed": len(ok), "failed": len(requests) - len(ok),
+            "elapsed_s": elapsed, "solves_per_s": len(ok) / elapsed,
             "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
             "ticks": ticks, "peak_live": peak_live, "peak_bytes": peak_bytes,
         }

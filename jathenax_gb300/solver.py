@@ -106,6 +106,14 @@ class Solve:
     def state(self):
         return _lib.read_clock(self.clock)
 
+    def box_sums(self):
+        """Float64 sums of every conserved component over the grid (run.py:186-187)."""
+        t = _lib.torch()
+        out = t.empty(self.desc.nvar, dtype=t.float64, device=self.S.device)
+        _lib.call("jx_box_sums", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(out),
+                  _lib.ptr(self.ws), self.nbytes, _lib.stream_handle())
+        return out.cpu().numpy()
+
     def as_jx_solve(self):
         """This solve as the C ABI's jx_solve (for batches)."""
         js = _lib.SolveStruct()

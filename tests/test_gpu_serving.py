@@ -36,3 +36,21 @@ def test_admission_holds_live_memory_under_the_budget():
     assert 0 < stats["peak_bytes"] <= budget
     assert stats["peak_live"] < 8
     assert all(r.finished >= r.admitted >= r.arrival for r in reqs)
+
+
+def test_a_failing_request_is_retired_and_the_others_complete():
+    """Host-side fault injection: one request starts with a NaN in its state."""
+    from jathenax_gb300.serve import Server, build_solve
+    reqs = small_stream(6, seed=11)
+    victim = reqs[2].rid
+
+    def builder(req, tile_y, clock=None, dtype=None):
+        solve = build_solve(req, tile_y, clock=clock, dtype=dtype)
+        if req.rid == victim:
+            solve.S[solve.S.shape[0] // 2, solve.S.shape[1] // 2, 1] = float("nan")
+        return solve
+
+    stats = Server(budget_bytes=1e9, steps_per_tick=2, builder=builder).run(reqs)
+    assert stats["failed"] == 1 and stats["completed"] == 5
+    assert reqs[2].error is not None and "non-finite" in reqs[2].error
+    assert all(r.error is None for r in reqs if r.rid != victim)
