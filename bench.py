@@ -371,7 +371,7 @@ def bench_batched(torch, tlim=0.02):
     reqs = [make_request(k, n, s, tlim, "float32", i) for i, (k, n, s) in enumerate(ensemble_specs())]
     tuned = autotune.tune("float32", "ppm4", "roe", 4, 1024)
     bank = ClockBank(len(reqs))
-    solves = [build_solve(r, tuned["tile_y"], clock=bank.slot(i)) for i, r in enumerate(reqs)]
+    solves = [build_solve(r, tuned["tile"], clock=bank.slot(i)) for i, r in enumerate(reqs)]
     batch = Batch(solves, blocks_per_sm=tuned["blocks_per_sm"], clocks=bank)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -395,7 +395,7 @@ def bench_batched(torch, tlim=0.02):
             "serial_fp64_solves_per_s": round(len(reqs) / serial_s, 3),
             "speedup": round(serial_s / batched_s, 2),
             "max_l1_density_err_fp32_vs_fp64": max(l1),
-            "tile_y": tuned["tile_y"], "blocks_per_sm": tuned["blocks_per_sm"],
+            "tile": tuned["tile"], "blocks_per_sm": tuned["blocks_per_sm"],
             "batched_s": round(batched_s, 3), "serial_s": round(serial_s, 3)}
 
 

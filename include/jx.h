@@ -51,7 +51,12 @@ typedef struct {
   int32_t ny, nx, nvar;   /* nvar >= 3; components 3.. are passive scalars */
   int32_t dtype;          /* jx_dtype */
   int32_t recon, rsolver, integrator;
-  int32_t tile_x, tile_y; /* 0 = library default; see jx_tile_info */
+  /* Stage tile. 0, 0 = library default: for 3/4 variables, float32 uses
+   * the register-marching kernel (58 x h tiles, h chosen per device) and
+   * float64 32 x 16 shared-memory tiles. tile_x = 58 selects marching
+   * tiles for 3/4 variables (tile_y >= 8 rows, or 0 for automatic). Any
+   * other tile_x x tile_y is a shared-memory tile. See jx_tile_info. */
+  int32_t tile_x, tile_y;
   double dx, dy, cs, dfloor;
   double viscosity, smagorinsky_cs, drag_rate;
 } jx_desc;
@@ -186,18 +191,19 @@ typedef struct {
 
 /* Batches advance many independent solves together (the reference evolves
  * one grid per evolve_isothermal call, run.py:20-69): per RK stage one
- * persistent launch per (precision, reconstruction, Riemann solver) group
- * walks a tile work list spanning all the group's grids. Solves must have 3
- * or 4 variables (16-byte aligned states for 4); tiles are 32 x tile_y and
- * each workspace must be sized for that tile (desc.tile_x = 32,
- * desc.tile_y = tile_y in jx_workspace_bytes). Results are bitwise the same
- * as running each solve alone with jx_step at the same tile.
+ * persistent launch per (precision, reconstruction, Riemann solver, kernel)
+ * group walks a tile work list spanning all the group's grids. Solves must
+ * have 3 or 4 variables (16-byte aligned states for 4). Each solve's
+ * desc.tile_x/tile_y select its tile as in jx_step, restricted to the two
+ * 3/4-variable kernels: 32 x h shared-memory tiles or 58 x h marching tiles
+ * (0, 0 = the default of jx_tile_info). Results are bitwise the same as
+ * running each solve alone with jx_step and the same descriptor.
  * jx_batch_plan writes a plan into host memory; copy it unchanged to device
  * memory of the same size and pass both to jx_batch_step, which enqueues one
  * evolve cycle of every solve (batched begin-step, renders, stages, kicks).
  * blocks_per_sm <= 0 picks the occupancy limit. */
-jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, int32_t tile_y, size_t* bytes);
-jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void* plan, size_t bytes);
+jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, size_t* bytes);
+jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t bytes);
 jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_per_sm, jx_stream s);
 /* Number of launch groups in a plan (-1 if not a plan). */
 int32_t jx_batch_groups(const void* plan);
@@ -241,7 +247,8 @@ jx_status jx_viscous_flux(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, con
 jx_status jx_box_sums(const jx_desc* d, const void* U, double* out, void* workspace,
                       size_t workspace_bytes, jx_stream s);
 
-/* Tile shape and shared memory the stage kernel will use for `d`. */
+/* Tile shape and shared memory the stage kernel will use for `d`
+ * (smem_bytes = 0 for marching tiles, which use registers and shuffles). */
 jx_status jx_tile_info(const jx_desc* d, int32_t* tile_x, int32_t* tile_y, int64_t* smem_bytes);
 
 /* modal_coefficients (forcing.py:63-100) on the host: the OU table

@@ -1,12 +1,13 @@
-"""Autotuner for the batched stage kernel.
+"""Autotuner for the batched stage kernels.
 
-Searches the tile height (32 x 8, 16 or 32 cells: the shared-memory tile and
-its halo, 256 threads each) and the number of persistent blocks per SM
-(occupancy limit or 1..4) for one (precision, reconstruction, Riemann solver,
-variable count) kernel class on a probe grid, timing a few evolve cycles of
-each candidate with CUDA events. The tile height never changes results (each
-cell's arithmetic is the same and the CFL reduction is an exact maximum), so
-the choice is purely about speed. Choices are cached per GPU model in
+Searches the stage tile (the shared-memory kernel's 32 x 8, 16 or 32 tiles
+of 256 threads, and the register-marching kernel's 58 x 16 / 32 / 64 tiles
+of 128 threads) and the number of persistent blocks per SM (occupancy limit
+or 1..4) for one (precision, reconstruction, Riemann solver, variable count)
+kernel class on a probe grid, timing a few evolve cycles of each candidate
+with CUDA events. Within one kernel the tile never changes results (each
+cell's arithmetic is the same and the CFL reduction is an exact maximum);
+the two kernels agree to rounding. Choices are cached per GPU model in
 memory and in ``$JATHENAX_GB300_CACHE`` (default
 ``~/.cache/jathenax_gb300/autotune.json``).
 """
@@ -17,7 +18,7 @@ from pathlib import Path
 
 from . import _lib
 
-TILE_HEIGHTS = (8, 16, 32)
+TILES = ((32, 8), (32, 16), (32, 32), (58, 16), (58, 32), (58, 64))
 BLOCKS_PER_SM = (0, 1, 2, 3, 4)
 _memory = {}
 
@@ -50,13 +51,13 @@ def _probe_state(nvar, side):
     return kelvin_helmholtz_tanh(side, side) if nvar == 4 else smooth_waves(side, side)
 
 
-def measure(dtype, reconstruct, rsolver, nvar, side, tile_y, blocks_per_sm, steps=4):
+def measure(dtype, reconstruct, rsolver, nvar, side, tile, blocks_per_sm, steps=4):
     """Milliseconds per evolve cycle of one probe solve run through the batch path."""
     t = _lib.torch()
     from .batch import Batch
     from .solver import Solve
     solve = Solve(_probe_state(nvar, side), 1.0 / side, 1.0 / side, 1.0, 1e-10, "rk3", 0.4, 1e30,
-                  2**31 - 1, reconstruct=reconstruct, rsolver=rsolver, tile=(32, tile_y),
+                  2**31 - 1, reconstruct=reconstruct, rsolver=rsolver, tile=tuple(tile),
                   dtype=getattr(t, dtype))
     batch = Batch([solve], blocks_per_sm=blocks_per_sm)
     for _ in range(2):
@@ -72,9 +73,9 @@ def measure(dtype, reconstruct, rsolver, nvar, side, tile_y, blocks_per_sm, step
 
 def tune(dtype="float32", reconstruct="ppm4", rsolver="roe", nvar=4, side=1024, steps=4,
          use_cache=True):
-    """Return {"tile_y": ..., "blocks_per_sm": ..., "ms_per_step": ..., "trials": [...]}."""
+    """Return {"tile": [tx, ty], "blocks_per_sm": ..., "ms_per_step": ..., "trials": [...]}."""
     t = _lib.torch()
-    key = "|".join(map(str, (t.cuda.get_device_name(), dtype, reconstruct, rsolver, nvar, side)))
+    key = "|".join(map(str, ("v2", t.cuda.get_device_name(), dtype, reconstruct, rsolver, nvar, side)))
     if use_cache:
         if key in _memory:
             return _memory[key]
@@ -83,13 +84,13 @@ def tune(dtype="float32", reconstruct="ppm4", rsolver="roe", nvar=4, side=1024, 
             _memory[key] = stored
             return stored
     trials = []
-    for tile_y in TILE_HEIGHTS:
+    for tile in TILES:
         for bps in BLOCKS_PER_SM:
             try:
-                ms = measure(dtype, reconstruct, rsolver, nvar, side, tile_y, bps, steps)
+                ms = measure(dtype, reconstruct, rsolver, nvar, side, tile, bps, steps)
             except (ValueError, RuntimeError):  # tile does not fit in shared memory
                 continue
-            trials.append({"tile_y": tile_y, "blocks_per_sm": bps, "ms_per_step": ms})
+            trials.append({"tile": list(tile), "blocks_per_sm": bps, "ms_per_step": ms})
     if not trials:
         raise RuntimeError("no autotuning candidate could run")
     best = min(trials, key=lambda r: r["ms_per_step"])

@@ -32,8 +32,8 @@ class ClockBank:
 class Batch:
     """Advance a list of :class:`jathenax_gb300.solver.Solve` together.
 
-    All solves must use the same tile (``tile=(32, tile_y)`` at construction)
-    and have 3 or 4 variables.
+    Solves have 3 or 4 variables; each keeps its own tile (the default, or
+    ``tile=(32, h)`` / ``tile=(104, h)`` at construction).
     """
 
     def __init__(self, solves, blocks_per_sm=0, clocks=None, plan_buffers=None):
@@ -41,16 +41,12 @@ class Batch:
         self.solves = list(solves)
         if not self.solves:
             raise ValueError("a batch needs at least one solve")
-        tiles = {(s.desc.tile_x or 32, s.desc.tile_y or 16) for s in self.solves}
-        if len(tiles) != 1 or next(iter(tiles))[0] != 32:
-            raise ValueError("batched solves must share one 32 x tile_y tile")
-        self.tile_y = next(iter(tiles))[1]
         self.blocks_per_sm = int(blocks_per_sm)
         self.clocks = clocks
         n = len(self.solves)
         arr = (_lib.SolveStruct * n)(*[s.as_jx_solve() for s in self.solves])
         size = ctypes.c_size_t()
-        _lib.call("jx_batch_plan_bytes", arr, n, self.tile_y, ctypes.byref(size))
+        _lib.call("jx_batch_plan_bytes", arr, n, ctypes.byref(size))
         nbytes = int(size.value)
         if plan_buffers is not None and plan_buffers[0].numel() >= nbytes:
             # Reused (host pinned, device) pair, e.g. a server re-planning every tick.
@@ -58,7 +54,7 @@ class Batch:
         else:
             self.plan_host = t.empty(nbytes, dtype=t.uint8).pin_memory()
             self.plan_dev = t.empty(nbytes, dtype=t.uint8, device=_lib.device())
-        _lib.call("jx_batch_plan", arr, n, self.tile_y, ctypes.c_void_p(self.plan_host.data_ptr()), nbytes)
+        _lib.call("jx_batch_plan", arr, n, ctypes.c_void_p(self.plan_host.data_ptr()), nbytes)
         # Stream-ordered copy: earlier steps that read an older plan in the same
         # buffer are enqueued before it.
         self.plan_dev.copy_(self.plan_host, non_blocking=True)

@@ -83,13 +83,73 @@ struct Tile {
   size_t smem;       // generic kernel
   bool fast_shape;   // 3/4 variables at tile width 32: the fast kernel applies
   size_t fast_smem;  // fast kernel
+  // Register-marching kernel (3/4 variables): kMarchTileX x mty tiles. The
+  // shared-memory tile above stays resolved for stages that fall back
+  // (trace outputs requested, 4-variable arrays not 16-byte aligned).
+  bool march;
+  int mty, mtiles_x, mtiles_y;
+  size_t cfl_slots;  // CFL partial slots the workspace holds
 };
 
-jx_status resolve_tile(const jx_desc* d, Tile* t) {
-  int tx = d->tile_x > 0 ? d->tile_x : 32;
-  int ty = d->tile_y > 0 ? d->tile_y : 16;
+int sm_count();
+
+// Resident marching blocks per SM for this descriptor on the current device
+// (cached; 4 when the device cannot be queried).
+int march_occupancy(const jx_desc* d) {
+  static int cache[64][2][5][3][2];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 4;
+  int& c = cache[dev][d->dtype][d->recon][d->rsolver][d->nvar - 3];
+  if (c == 0) {
+    int n = 0;
+    switch (d->recon) {
+      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, false); break;
+      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, false); break;
+      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, false); break;
+      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, false); break;
+      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, false); break;
+    }
+    if (n < 1) {
+      cudaGetLastError();
+      return 4;
+    }
+    c = n;
+  }
+  return c;
+}
+
+// Rows of an automatic marching tile: the height whose tiles, spread over
+// the resident warp slots of the device, finish soonest. A tile of h rows
+// costs about h + 2.5 row-updates (the 6 leading rows of the walk do the y
+// work only); the grid runs in ceil(tiles / slots) rounds.
+int march_rows(const jx_desc* d) {
+  static const int kRows[] = {8, 12, 16, 24, 32, 48, 64};
+  const int64_t slots = (int64_t)sm_count() * march_occupancy(d) * kMarchWarps;
+  const int64_t cols = (d->nx + kMarchTileX - 1) / kMarchTileX;
+  int best = kRows[0];
+  double best_cost = 1e300;
+  for (int h : kRows) {
+    const int64_t tiles = cols * ((d->ny + h - 1) / h);
+    const int64_t rounds = (tiles + slots - 1) / slots;
+    const double cost = (double)rounds * (h + 2.5);
+    if (cost <= best_cost) {
+      best_cost = cost;
+      best = h;
+    }
+  }
+  return best;
+}
+
+jx_status resolve_tile(const jx_desc* d, Tile* t, bool device = true) {
+  // Automatic tiles: float32 marches; float64, bound by the FP64 pipe,
+  // keeps the shared-memory tile, which evaluates no halo faces twice.
+  const bool three_four = d->nvar == 3 || d->nvar == 4;
+  const bool march = three_four && (d->tile_x == kMarchTileX ||
+                                    (d->tile_x == 0 && d->tile_y == 0 && d->dtype == JX_F32));
+  int tx = d->tile_x > 0 && !march ? d->tile_x : 32;
+  int ty = d->tile_y > 0 && !march ? d->tile_y : 16;
   size_t smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
-  if (d->tile_x == 0 && d->tile_y == 0) {
+  if (march || (d->tile_x == 0 && d->tile_y == 0)) {
     while (smem > kSmemDefaultCap && ty > 4) {
       ty /= 2;
       smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
@@ -101,7 +161,7 @@ jx_status resolve_tile(const jx_desc* d, Tile* t) {
   }
   if (smem > kSmemLimit)
     return fail(JX_ERR_INVALID, "tile %dx%d needs %zu bytes of shared memory (limit %zu)", tx, ty, smem, kSmemLimit);
-  t->fast_shape = (d->nvar == 3 || d->nvar == 4) && tx == 32;
+  t->fast_shape = three_four && tx == 32;
   t->fast_smem = t->fast_shape ? fast_smem_bytes(d->recon, d->dtype, ty) : 0;
   if (t->fast_smem > kSmemLimit)
     return fail(JX_ERR_INVALID, "tile 32x%d needs %zu bytes of shared memory (limit %zu)", ty, t->fast_smem,
@@ -112,6 +172,23 @@ jx_status resolve_tile(const jx_desc* d, Tile* t) {
   t->tiles_y = (d->ny + ty - 1) / ty;
   t->smem = smem;
   if ((int64_t)t->tiles_x * t->tiles_y > ((int64_t)1 << 31) - 1) return fail(JX_ERR_INVALID, "too many tiles");
+  t->march = march;
+  t->mty = t->mtiles_x = t->mtiles_y = 0;
+  size_t slots = (size_t)t->tiles_x * t->tiles_y;
+  if (march) {
+    if (d->tile_y > 0 && d->tile_y < kMarchMinRows)
+      return fail(JX_ERR_INVALID, "marching tiles need at least %d rows", kMarchMinRows);
+    // The workspace covers the shortest automatic marching tile, so its
+    // size does not depend on the device.
+    const int64_t cols = (d->nx + kMarchTileX - 1) / kMarchTileX;
+    const int rows_min = d->tile_y > 0 ? d->tile_y : kMarchMinRows;
+    const size_t mslots = (size_t)(cols * ((d->ny + rows_min - 1) / rows_min));
+    if (mslots > slots) slots = mslots;
+    t->mty = d->tile_y > 0 ? d->tile_y : (device ? march_rows(d) : kMarchMinRows);
+    t->mtiles_x = (int)cols;
+    t->mtiles_y = (d->ny + t->mty - 1) / t->mty;
+  }
+  t->cfl_slots = slots;
   return JX_OK;
 }
 
@@ -125,7 +202,7 @@ Layout layout_for(const jx_desc* d, const Tile& t) {
   L.scal = off;
   off += 256;
   L.cfl = off;
-  size_t slots = (size_t)t.tiles_x * t.tiles_y;
+  size_t slots = t.cfl_slots;
   if (slots < (size_t)kCflBlocksMax) slots = kCflBlocksMax;
   off = align256(off + slots * kCflSlots * sizeof(double));
   L.p1 = off;
@@ -190,7 +267,32 @@ CflParams cfl_params(const jx_desc* d, const void* X, const jx_clock* clock, con
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
+// The marching kernel applies unless trace outputs are requested (it writes
+// none) or a 4-variable array is not 16-byte aligned (128-bit accesses).
+bool use_march(const jx_desc* d, const StageParams& p, const Tile& t) {
+  return t.march && !p.trace_on &&
+         (d->nvar == 3 ||
+          (aligned16(p.U) && aligned16(p.V) && aligned16(p.Uout) && (p.Vout == nullptr || aligned16(p.Vout))));
+}
+
+cudaError_t launch_march(int recon, int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
+  switch (recon) {
+    case JX_DC: return launch_march_dc(dtype, rsolver, p, grid, s);
+    case JX_PLM: return launch_march_plm(dtype, rsolver, p, grid, s);
+    case JX_PPM4: return launch_march_ppm4(dtype, rsolver, p, grid, s);
+    case JX_PPMX: return launch_march_ppmx(dtype, rsolver, p, grid, s);
+    default: return launch_march_wenoz(dtype, rsolver, p, grid, s);
+  }
+}
+
 cudaError_t launch_stage(const jx_desc* d, const StageParams& p, const Tile& t, cudaStream_t s) {
+  if (use_march(d, p, t)) {
+    StageParams m = p;
+    m.tx = kMarchTileX;
+    m.ty = t.mty;
+    m.tiles_x = t.mtiles_x;
+    return launch_march(d->recon, d->dtype, d->rsolver, m, dim3((unsigned)((int64_t)t.mtiles_x * t.mtiles_y)), s);
+  }
   dim3 grid((unsigned)((int64_t)t.tiles_x * t.tiles_y));
   // The fast kernel reads/writes 4-variable cells with 128-bit accesses.
   const bool fast = t.fast_shape && (d->nvar == 3 || (aligned16(p.U) && aligned16(p.V) && aligned16(p.Uout) &&
@@ -329,9 +431,9 @@ jx_status jx_tile_info(const jx_desc* d, int32_t* tile_x, int32_t* tile_y, int64
   if (st) return st;
   Tile t;
   if ((st = resolve_tile(d, &t))) return st;
-  if (tile_x) *tile_x = t.tx;
-  if (tile_y) *tile_y = t.ty;
-  if (smem_bytes) *smem_bytes = (int64_t)t.smem;
+  if (tile_x) *tile_x = t.march ? kMarchTileX : t.tx;
+  if (tile_y) *tile_y = t.march ? t.mty : t.ty;
+  if (smem_bytes) *smem_bytes = t.march ? 0 : (int64_t)t.smem;
   return JX_OK;
 }
 
@@ -340,7 +442,7 @@ jx_status jx_workspace_bytes(const jx_desc* d, size_t* bytes) {
   if (st) return st;
   if (!bytes) return fail(JX_ERR_INVALID, "null output pointer");
   Tile t;
-  if ((st = resolve_tile(d, &t))) return st;
+  if ((st = resolve_tile(d, &t, false))) return st;
   *bytes = layout_for(d, t).total;
   return JX_OK;
 }
@@ -559,10 +661,11 @@ jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sin
 namespace {
 
 constexpr uint32_t kPlanMagic = 0x4a584250;  // "JXBP"
-constexpr int kMaxGroups = 30;
+constexpr int kMaxGroups = 90;  // 2 precisions x 5 reconstructions x 3 solvers x 3 kernel/count classes
 
 struct BatchGroup {
-  int dtype, recon, rsolver, first, count, tile_first, nwork, pad;
+  int dtype, recon, rsolver, first, count, tile_first, nwork, march;
+  int nv, pad;  // marching groups: the variable count of every solve (0 in shared-memory groups)
   size_t smem;
 };
 
@@ -573,7 +676,7 @@ struct BatchSolveInfo {
 
 struct BatchPlanHeader {
   uint32_t magic;
-  int32_t n, n_groups, max_stages, tile_y, pad;
+  int32_t n, n_groups, max_stages, pad;
   int64_t bytes, off_params, off_offsets, off_begin, off_info;
   BatchGroup groups[kMaxGroups];
 };
@@ -631,19 +734,41 @@ cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* p
   }
 }
 
-jx_status check_batch_solve(int i, const jx_solve& in, int tile_y, jx_solve* out, Tile* t, Ws* w) {
-  *out = in;
-  out->desc.tile_x = 32;
-  out->desc.tile_y = tile_y;
-  jx_status st = check_desc(&out->desc);
+int batch_march_occupancy(int recon, int dtype, int rsolver, int nv) {
+  switch (recon) {
+    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, true);
+    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, true);
+    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, true);
+    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, true);
+    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, true);
+  }
+}
+
+cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, const StageParams* params,
+                               const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+  switch (recon) {
+    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    default: return launch_batch_march_wenoz(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+  }
+}
+
+jx_status check_batch_solve(int i, const jx_solve& in, Tile* t, Ws* w) {
+  jx_status st = check_desc(&in.desc);
   if (st) return fail(st, "solve %d: %s", i, jx_last_error());
-  const jx_desc& d = out->desc;
+  const jx_desc& d = in.desc;
   if (d.nvar != 3 && d.nvar != 4) return fail(JX_ERR_INVALID, "solve %d: batches take 3 or 4 variables", i);
   if (!in.S || !in.A || !in.B || !in.clock) return fail(JX_ERR_INVALID, "solve %d: null state or clock", i);
   if (in.S == in.A || in.S == in.B || in.A == in.B) return fail(JX_ERR_INVALID, "solve %d: S, A, B must differ", i);
   if (d.nvar == 4 && !(aligned16(in.S) && aligned16(in.A) && aligned16(in.B)))
     return fail(JX_ERR_INVALID, "solve %d: 4-variable states must be 16-byte aligned", i);
   if ((st = resolve_tile(&d, t))) return fail(st, "solve %d: %s", i, jx_last_error());
+  if (!t->march && !t->fast_shape)
+    return fail(JX_ERR_INVALID, "solve %d: batch tiles are 32 x h or %d x h, not %d x %d", i, kMarchTileX, t->tx,
+                t->ty);
+  if (!t->march && t->ty > 64) return fail(JX_ERR_INVALID, "solve %d: batch tiles have at most 64 rows", i);
   if ((st = bind_ws(&d, *t, in.workspace, in.workspace_bytes, w))) return fail(st, "solve %d: %s", i, jx_last_error());
   if (in.forcing.raw_force && (!in.forcing.table || !in.forcing.cos_x || !in.forcing.sin_x || !in.forcing.cos_y ||
                                !in.forcing.sin_y || in.forcing.n_modes < 1 || in.forcing.n_updates < 1))
@@ -655,16 +780,15 @@ jx_status check_batch_solve(int i, const jx_solve& in, int tile_y, jx_solve* out
 
 extern "C" {
 
-jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, int32_t tile_y, size_t* bytes) {
+jx_status jx_batch_plan_bytes(const jx_solve* solves, int32_t n, size_t* bytes) {
   if (!solves || n < 1 || !bytes) return fail(JX_ERR_INVALID, "a batch needs at least one solve");
-  if (tile_y < 1 || tile_y > 64) return fail(JX_ERR_INVALID, "tile_y must be in [1, 64]");
   *bytes = plan_layout(n).total;
   return JX_OK;
 }
 
-jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void* plan, size_t bytes) {
+jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t bytes) {
   size_t need = 0;
-  jx_status st = jx_batch_plan_bytes(solves, n, tile_y, &need);
+  jx_status st = jx_batch_plan_bytes(solves, n, &need);
   if (st) return st;
   if (!plan || bytes < need) return fail(JX_ERR_WORKSPACE, "plan buffer has %zu bytes, needs %zu", bytes, need);
   const PlanLayout L = plan_layout(n);
@@ -673,7 +797,6 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void*
   BatchPlanHeader* h = reinterpret_cast<BatchPlanHeader*>(base);
   h->magic = kPlanMagic;
   h->n = n;
-  h->tile_y = tile_y;
   h->bytes = (int64_t)need;
   h->off_params = (int64_t)L.params;
   h->off_offsets = (int64_t)L.offsets;
@@ -685,20 +808,25 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void*
   BatchSolveInfo* info = reinterpret_cast<BatchSolveInfo*>(base + L.info);
 
   // Validate every solve once, then group by (precision, reconstruction,
-  // Riemann solver) in order of first appearance; solves keep their relative
-  // order inside a group.
-  std::vector<jx_solve> sv(n);
+  // Riemann solver, kernel; and variable count for the marching kernel,
+  // which is compiled per count) in order of first appearance; solves keep
+  // their relative order inside a group. A shared-memory group launches with
+  // the largest tile of its solves; each solve walks its own tiles.
+  std::vector<jx_solve> sv(solves, solves + n);
   std::vector<Tile> tl(n);
   std::vector<Ws> wl(n);
   for (int i = 0; i < n; ++i)
-    if ((st = check_batch_solve(i, solves[i], tile_y, &sv[i], &tl[i], &wl[i]))) return st;
+    if ((st = check_batch_solve(i, solves[i], &tl[i], &wl[i]))) return st;
   std::vector<int> group_of(n, -1);
   int n_groups = 0;
   for (int i = 0; i < n; ++i) {
     const jx_desc& d = sv[i].desc;
+    const int march = tl[i].march ? 1 : 0;
+    const int nv = march ? d.nvar : 0;
     int g = 0;
     while (g < n_groups && !(h->groups[g].dtype == d.dtype && h->groups[g].recon == d.recon &&
-                             h->groups[g].rsolver == d.rsolver))
+                             h->groups[g].rsolver == d.rsolver && h->groups[g].march == march &&
+                             h->groups[g].nv == nv))
       ++g;
     if (g == n_groups) {
       if (n_groups == kMaxGroups) return fail(JX_ERR_INVALID, "more than %d solver groups", kMaxGroups);
@@ -706,8 +834,11 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void*
       G.dtype = d.dtype;
       G.recon = d.recon;
       G.rsolver = d.rsolver;
-      G.smem = fast_smem_bytes(d.recon, d.dtype, tile_y);
+      G.march = march;
+      G.nv = nv;
+      G.smem = 0;
     }
+    if (!march && tl[i].fast_smem > h->groups[g].smem) h->groups[g].smem = tl[i].fast_smem;
     group_of[i] = g;
   }
   int order_count = 0, next_int = 0;
@@ -731,7 +862,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void*
       I.n_stages = nst;
       if (nst > h->max_stages) h->max_stages = nst;
       offsets[next_int++] = tiles;
-      tiles += t.tiles_x * t.tiles_y;
+      tiles += G.march ? t.mtiles_x * t.mtiles_y : t.tiles_x * t.tiles_y;
       BeginParams& B = begin[k];
       B.q = dt_params(&d);
       B.clock = sv[i].clock;
@@ -750,6 +881,11 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, int32_t tile_y, void*
         void* out = stage == nst ? sv[i].S : (stage % 2 == 1 ? sv[i].A : sv[i].B);
         P = make_stage_params(&d, t, w, stage, in, sv[i].S, out, stage == nst ? nullptr : sv[i].S, nullptr,
                               forced, sv[i].clock, nullptr);
+        if (G.march) {
+          P.tx = kMarchTileX;
+          P.ty = t.mty;
+          P.tiles_x = t.mtiles_x;
+        }
         in = out;
       }
     }
@@ -782,16 +918,22 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
     for (int g = 0; g < h->n_groups; ++g) {
       const BatchGroup& G = h->groups[g];
       int bps = blocks_per_sm;
-      if (bps <= 0) bps = batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
+      if (bps <= 0)
+        bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv)
+                      : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
       if (bps < 1) bps = 1;
       int64_t blocks = (int64_t)sms * bps;
-      if (blocks > G.nwork) blocks = G.nwork;
+      const int64_t per_block = G.march ? kMarchWarps : 1;  // marching blocks take one tile per warp
+      if (blocks > (G.nwork + per_block - 1) / per_block) blocks = (G.nwork + per_block - 1) / per_block;
       if (blocks < 1) continue;
-      if ((st = cuda_check(launch_batch(G.recon, G.dtype, G.rsolver, params_dev + (size_t)(stage - 1) * h->n + G.first,
-                                        offsets_dev + G.tile_first, G.count, G.nwork, dim3((unsigned)blocks), G.smem,
-                                        s),
-                           "batched stage kernel")))
-        return st;
+      const StageParams* P = params_dev + (size_t)(stage - 1) * h->n + G.first;
+      const int* offs = offsets_dev + G.tile_first;
+      const cudaError_t e =
+          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, P, offs, G.count, G.nwork,
+                                       dim3((unsigned)blocks), s)
+                  : launch_batch(G.recon, G.dtype, G.rsolver, P, offs, G.count, G.nwork, dim3((unsigned)blocks),
+                                 G.smem, s);
+      if ((st = cuda_check(e, "batched stage kernel"))) return st;
     }
   }
   for (int i = 0; i < h->n; ++i) {

@@ -112,6 +112,31 @@ inline size_t fast_smem_bytes(int recon, int dtype, int ty) {
   return (w + fx + fy + a + r) * 4 * (dtype == JX_F64 ? 8 : 4);
 }
 
+// Register-marching stage kernel (jx_stage_march.cuh): one warp per tile of
+// kMarchTileX columns by StageParams::ty rows (two columns per lane, 3 ghost
+// columns per side of the 64-column strip). Blocks are single warps: the
+// warps share nothing, and the SM's register file then holds as many warps
+// as registers allow (no rounding to whole multi-warp blocks).
+constexpr int kMarchWarps = 1;
+constexpr int kMarchTileX = 58;
+constexpr int kMarchMinRows = 8;
+
+cudaError_t launch_march_dc(int, int, const StageParams&, dim3, cudaStream_t);
+cudaError_t launch_march_plm(int, int, const StageParams&, dim3, cudaStream_t);
+cudaError_t launch_march_ppm4(int, int, const StageParams&, dim3, cudaStream_t);
+cudaError_t launch_march_ppmx(int, int, const StageParams&, dim3, cudaStream_t);
+cudaError_t launch_march_wenoz(int, int, const StageParams&, dim3, cudaStream_t);
+cudaError_t launch_batch_march_dc(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_plm(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppm4(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppmx(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_wenoz(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, bool batch);
+int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, bool batch);
+int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, bool batch);
+int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, bool batch);
+int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, bool batch);
+
 typedef cudaError_t (*FaceStatesLauncher)(int dtype, const void* W, int ny, int nx, int nv,
                                           int axis, double dfloor, void* left, void* right,
                                           cudaStream_t s);

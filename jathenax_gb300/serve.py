@@ -65,14 +65,18 @@ def make_stream(n, rate, seed=0, side_range=(64, 2048), tlim_range=(0.2, 3.0), f
     return out
 
 
-def build_solve(req, tile_y=16, clock=None, dtype=None):
-    """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163)."""
+def build_solve(req, tile=(0, 0), clock=None, dtype=None):
+    """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163).
+
+    ``tile`` (0, 0) is the library default: marching tiles in float32,
+    shared-memory tiles in float64.
+    """
     t = _lib.torch()
     from .forcing import cartesian_modes, forcing_basis, modal_coefficients
     from .initial_conditions import cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest
     from .solver import Solve
     n = req.side
-    kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver, tile=(32, tile_y),
+    kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver, tile=tuple(tile),
               dtype=getattr(t, dtype or req.dtype), clock=clock)
     if req.problem == "kh":
         return Solve(kelvin_helmholtz_tanh(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
@@ -105,16 +109,16 @@ def footprint_bytes(req, dtype=None):
 class Server:
     """Continuous-batching request loop with an HBM admission budget."""
 
-    def __init__(self, budget_bytes=150e9, tile_y=16, steps_per_tick=4, blocks_per_sm=0,
+    def __init__(self, budget_bytes=150e9, tile=(0, 0), steps_per_tick=4, blocks_per_sm=0,
                  max_live=1024, keep_results=False, dtype=None, builder=None):
         self.budget = float(budget_bytes)
-        self.tile_y = tile_y
+        self.tile = tuple(tile)
         self.steps_per_tick = steps_per_tick
         self.blocks_per_sm = blocks_per_sm
         self.max_live = max_live
         self.keep_results = keep_results
         self.dtype = dtype  # serve every request in this precision (None: as requested)
-        self.builder = builder or build_solve  # (request, tile_y, clock, dtype) -> Solve
+        self.builder = builder or build_solve  # (request, tile, clock, dtype) -> Solve
 
     def run(self, requests):
         """Serve `requests` (arrival-ordered or not); returns a stats dict."""
@@ -142,7 +146,7 @@ class Server:
                    and in_use + footprint_bytes(pending[0], self.dtype) <= self.budget):
                 req = pending.popleft()
                 slot = free_slots.pop()
-                solve = self.builder(req, self.tile_y, clock=bank.slot(slot), dtype=self.dtype)
+                solve = self.builder(req, self.tile, clock=bank.slot(slot), dtype=self.dtype)
                 req.admitted = time.perf_counter() - t0
                 live.append((req, solve, slot))
                 in_use += footprint_bytes(req, self.dtype)

@@ -66,9 +66,19 @@ def test_workspace_and_tiles():
     assert lib.jx_workspace_bytes(ctypes.byref(_desc()), ctypes.byref(size)) == 0
     assert size.value % 256 == 0 and size.value > 0
     tx, ty, smem = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+    # float32 with 3/4 variables defaults to the register-marching kernel
+    # (58-column tiles), float64 to the 32-column shared-memory tile.
+    assert lib.jx_tile_info(ctypes.byref(_desc(nvar=4, dtype=_lib.JX_F32)), ctypes.byref(tx),
+                            ctypes.byref(ty), ctypes.byref(smem)) == 0
+    assert tx.value == 58 and 8 <= ty.value <= 64 and smem.value == 0
     assert lib.jx_tile_info(ctypes.byref(_desc(nvar=4)), ctypes.byref(tx), ctypes.byref(ty),
                             ctypes.byref(smem)) == 0
     assert (tx.value, ty.value) == (32, 16) and smem.value <= 112 * 1024
+    assert lib.jx_tile_info(ctypes.byref(_desc(nvar=4, tile_x=32, tile_y=16)), ctypes.byref(tx),
+                            ctypes.byref(ty), ctypes.byref(smem)) == 0
+    assert (tx.value, ty.value) == (32, 16) and smem.value <= 112 * 1024
+    assert lib.jx_tile_info(ctypes.byref(_desc(nvar=3, tile_x=58, tile_y=4)), ctypes.byref(tx),
+                            ctypes.byref(ty), ctypes.byref(smem)) == _lib.JX_ERR_INVALID
     # Many scalars shrink the default tile to keep two CTAs per SM.
     assert lib.jx_tile_info(ctypes.byref(_desc(nvar=12)), ctypes.byref(tx), ctypes.byref(ty),
                             ctypes.byref(smem)) == 0

@@ -6,14 +6,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def make_solve(kind, n, dtype, recon, rsolver, integrator, tlim, tile_y, clock=None, seed=1618):
+def make_solve(kind, n, dtype, recon, rsolver, integrator, tlim, tile_y, clock=None, seed=1618, tile_x=32):
     import torch
     from jathenax_gb300.forcing import cartesian_modes, forcing_basis, modal_coefficients
     from jathenax_gb300.initial_conditions import (
         cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest)
     from jathenax_gb300.solver import Solve
     tdtype = getattr(torch, dtype)
-    kw = dict(reconstruct=recon, rsolver=rsolver, tile=(32, tile_y), dtype=tdtype, clock=clock)
+    kw = dict(reconstruct=recon, rsolver=rsolver, tile=(tile_x, tile_y), dtype=tdtype, clock=clock)
     if kind == "kh":
         U = kelvin_helmholtz_tanh(n, n)
         return Solve(U, 1 / n, 1 / n, 1.0, 1e-10, integrator, 0.4, tlim, 10**6, **kw)
@@ -41,41 +41,64 @@ SPECS = [  # kind, n, dtype, recon, rsolver, integrator, tlim
 ]
 
 
-def run_alone(spec, tile_y):
-    s = make_solve(*spec, tile_y=tile_y)
+def run_alone(spec, tile_y, tile_x=32):
+    s = make_solve(*spec, tile_y=tile_y, tile_x=tile_x)
     s.run(steps_per_sync=8)
     c = s.state()
     return s.S.cpu().numpy(), c.time, c.cycle
 
 
-@pytest.mark.parametrize("tile_y", [16])
-def test_batch_results_equal_solo_results_bitwise(tile_y):
+@pytest.mark.parametrize("tile", [(32, 16), (58, 16), (0, 0)])
+def test_batch_results_equal_solo_results_bitwise(tile):
     from jathenax_gb300.batch import Batch, ClockBank
+    tile_x, tile_y = tile
     bank = ClockBank(len(SPECS))
-    solves = [make_solve(*spec, tile_y=tile_y, clock=bank.slot(i)) for i, spec in enumerate(SPECS)]
+    solves = [make_solve(*spec, tile_y=tile_y, tile_x=tile_x, clock=bank.slot(i)) for i, spec in enumerate(SPECS)]
     batch = Batch(solves, clocks=bank)
-    assert batch.groups == 4
+    # 4 (precision, method) classes; marching groups split by variable count
+    assert batch.groups == {(32, 16): 4, (58, 16): 5, (0, 0): 5}[tile]
     clocks = batch.run(steps_per_sync=8)
     for spec, s, c in zip(SPECS, solves, clocks):
-        U_alone, t_alone, cyc_alone = run_alone(spec, tile_y)
+        U_alone, t_alone, cyc_alone = run_alone(spec, tile_y, tile_x)
         assert c.done and c.cycle == cyc_alone and c.time == t_alone, spec
         np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=str(spec))
 
 
-def test_batch_tile_height_does_not_change_results():
+@pytest.mark.parametrize("tile_x", [32, 58])
+def test_batch_tile_height_does_not_change_results(tile_x):
     from jathenax_gb300.batch import Batch
     outs = []
     for tile_y in (8, 32):
-        solves = [make_solve(*spec, tile_y=tile_y) for spec in SPECS[:4]]
+        solves = [make_solve(*spec, tile_y=tile_y, tile_x=tile_x) for spec in SPECS[:4]]
         Batch(solves, blocks_per_sm=2).run(steps_per_sync=4, use_graph=False)
         outs.append([s.S.cpu().numpy() for s in solves])
     for a, b in zip(*outs):
         np.testing.assert_array_equal(a, b)
 
 
-def test_batch_rejects_mixed_tiles_and_wide_states():
+def test_batch_mixes_tiles_and_kernels_bitwise():
+    """Solves of one group with different tiles, and both kernels side by side."""
     from jathenax_gb300.batch import Batch
-    a = make_solve("kh", 32, "float32", "ppm4", "roe", "rk3", 0.01, tile_y=16)
-    b = make_solve("kh", 32, "float32", "ppm4", "roe", "rk3", 0.01, tile_y=8)
-    with pytest.raises(ValueError, match="share one"):
-        Batch([a, b])
+    tiles = [(32, 16), (32, 8), (58, 8), (58, 32), (0, 0), (32, 32), (58, 64)]
+    solves = [make_solve(*spec, tile_y=ty, tile_x=tx) for spec, (tx, ty) in zip(SPECS, tiles)]
+    batch = Batch(solves)
+    assert batch.groups == 5  # the float32 ppm4/roe class runs both kernels
+    batch.run(steps_per_sync=4)
+    for spec, s, (tx, ty) in zip(SPECS, solves, tiles):
+        U_alone, _, _ = run_alone(spec, ty, tx)
+        np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=f"{spec} {tx}x{ty}")
+
+
+def test_batch_rejects_other_tiles_and_wide_states():
+    from jathenax_gb300.batch import Batch
+    import torch
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from jathenax_gb300.solver import Solve
+    a = make_solve("kh", 32, "float32", "ppm4", "roe", "rk3", 0.01, tile_y=16, tile_x=16)
+    with pytest.raises(ValueError, match="batch tiles"):
+        Batch([a])
+    U = kelvin_helmholtz_tanh(32, 32)
+    wide = Solve(np.concatenate([U, U[..., 3:]], axis=-1), 1 / 32, 1 / 32, 1.0, 1e-10, "rk3", 0.4, 0.01, 10,
+                 dtype=torch.float32)
+    with pytest.raises(ValueError, match="3 or 4 variables"):
+        Batch([wide])

@@ -1,0 +1,113 @@
+"""The register-marching stage kernel (58-column tiles) against the
+shared-memory tile kernel (32-column tiles) and the float64 oracle.
+
+Both kernels evaluate every face and cell with the same device functions in
+the same order; where they can still differ is the compiler's contraction of
+a multiply and an add into one FMA, which depends on how often a product is
+reused (with donor-cell edges the x and y Riemann problems of a cell share
+products). So the two kernels are compared at the step tolerance in float64
+(and 1e-5 of each component's largest magnitude in float32), over every
+reconstruction and Riemann solver, the viscous, drag and SGS-stress terms,
+RK4's saved-register stages and ragged and tiny periodic grids (fewer cells
+than one strip or one tile); the marching kernel against itself is bitwise
+for every tile height.
+"""
+
+import numpy as np
+import pytest
+from conftest import STEP_RTOL, assert_rel
+
+from oracle import hydro_oracle as H
+from test_gpu_parity import RECONS, SOLVERS, noisy_state
+
+pytestmark = pytest.mark.gpu
+
+
+def stepped(U0, dtype, tile, integrator="rk3", steps=1, dt=0.001, recon="ppm4", rsolver="roe", tau=None,
+            **kw):
+    import torch
+    from jathenax_gb300 import _lib
+    from jathenax_gb300 import hydro as G
+    ny, nx = U0.shape[:2]
+    desc = G.make_desc(U0.shape, dtype, 1 / nx, 1 / ny, 1.0, 1e-10, integrator, reconstruct=recon,
+                       rsolver=rsolver, tile=tile, **kw)
+    ws, nbytes = _lib.workspace(desc)
+    U = torch.as_tensor(U0, device="cuda").to(dtype)
+    predict = None
+    if tau is not None:
+        T = torch.as_tensor(tau, device="cuda").to(dtype)
+        predict = lambda w, W: w * T  # noqa: E731 - a fixed stress field
+    for _ in range(steps):
+        clock = _lib.new_clock(dt=dt)
+        U, _ = G.run_stages(desc, U, clock=clock, ws=ws, nbytes=nbytes, predict_stress=predict,
+                            sgs_weights=torch.ones((), device="cuda", dtype=dtype) if tau is not None else None)
+    return U.cpu().numpy()
+
+
+def assert_close(a, b, what):
+    assert_rel(a, b, STEP_RTOL if a.dtype == np.float64 else 1e-5, what)
+
+
+def assert_bitwise(a, b, what):
+    assert a.dtype == b.dtype and a.shape == b.shape, what
+    same = a.view(np.uint8).reshape(a.shape + (-1,)) == b.view(np.uint8).reshape(b.shape + (-1,))
+    bad = np.argwhere(~np.all(same, axis=-1))
+    assert len(bad) == 0, f"{what}: {len(bad)} values differ, first at {bad[:3].tolist()}"
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("rs", SOLVERS)
+@pytest.mark.parametrize("rec", RECONS)
+def test_marching_matches_tile_kernel(rec, rs, dtype):
+    import torch
+    U0 = noisy_state(213, 77, nvar=4, seed=RECONS.index(rec) * 3 + SOLVERS.index(rs))
+    td = getattr(torch, dtype)
+    a = stepped(U0, td, (58, 16), recon=rec, rsolver=rs, steps=2)
+    b = stepped(U0, td, (32, 16), recon=rec, rsolver=rs, steps=2)
+    assert_close(a, b, f"{rec}/{rs}/{dtype}")
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("integrator", ["rk2", "rk4"])
+def test_marching_viscous_drag_three_variables(integrator, dtype):
+    import torch
+    U0 = noisy_state(150, 61, nvar=3, seed=4)
+    td = getattr(torch, dtype)
+    kw = dict(viscosity=2e-3, smagorinsky_cs=0.2, drag_rate=0.3)
+    a = stepped(U0, td, (58, 12), integrator=integrator, rsolver="hlle", **kw)
+    b = stepped(U0, td, (32, 8), integrator=integrator, rsolver="hlle", **kw)
+    assert_close(a, b, f"{integrator}/{dtype}")
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_marching_sgs_stress(dtype):
+    import torch
+    U0 = noisy_state(120, 40, nvar=4, seed=8)
+    tau = 1e-3 * np.random.default_rng(3).standard_normal((40, 120, 3))
+    td = getattr(torch, dtype)
+    a = stepped(U0, td, (58, 8), recon="wenoz", tau=tau)
+    b = stepped(U0, td, (32, 16), recon="wenoz", tau=tau)
+    assert_close(a, b, dtype)
+
+
+@pytest.mark.parametrize("shape", [(5, 7), (1, 40), (33, 1), (9, 59), (9, 105), (70, 26), (64, 116)])
+def test_marching_tiny_and_ragged_grids(shape):
+    import torch
+    ny, nx = shape
+    U0 = noisy_state(nx, ny, nvar=4, seed=ny + nx)
+    for rec in ("ppm4", "wenoz", "plm", "dc"):
+        a = stepped(U0, torch.float64, (58, 8), recon=rec)
+        b = stepped(U0, torch.float64, (32, 16), recon=rec)
+        assert_close(a, b, f"{shape} {rec}")
+        ref = H.step(U0, 0.001, 1 / nx, 1 / ny, 1.0, 1e-10, "rk3", recon=rec)
+        assert_rel(a, ref, STEP_RTOL, f"{shape} {rec} vs oracle")
+
+
+def test_marching_tile_height_does_not_change_results():
+    import torch
+    U0 = noisy_state(300, 190, nvar=4, seed=12)
+    base = stepped(U0, torch.float32, (58, 8), steps=3)
+    for rows in (12, 16, 24, 32, 48, 64, 100):
+        assert_bitwise(stepped(U0, torch.float32, (58, rows), steps=3), base, f"rows {rows}")
+    # The automatic tile (device-dependent height) gives the same state too.
+    assert_bitwise(stepped(U0, torch.float32, (0, 0), steps=3), base, "automatic tile")

@@ -44,8 +44,8 @@ def test_a_failing_request_is_retired_and_the_others_complete():
     reqs = small_stream(6, seed=11)
     victim = reqs[2].rid
 
-    def builder(req, tile_y, clock=None, dtype=None):
-        solve = build_solve(req, tile_y, clock=clock, dtype=dtype)
+    def builder(req, tile, clock=None, dtype=None):
+        solve = build_solve(req, tile, clock=clock, dtype=dtype)
         if req.rid == victim:
             solve.S[solve.S.shape[0] // 2, solve.S.shape[1] // 2, 1] = float("nan")
         return solve
