@@ -16,6 +16,7 @@ path) and the value is the sum over ranks.
 """
 
 import argparse
+import ctypes
 import csv
 import io
 import json
@@ -236,7 +237,9 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(es.elapsed_time(ee), world)
     state_bytes = host_in.numel() * host_in.element_size()
-    return dict(value=value, ms=ms, stage_ms=stage_ms, clocks=clock_info, solve_state=state,
+    tx, ty, smem = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+    _lib.call("jx_tile_info", ctypes.byref(solve.desc), ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(smem))
+    return dict(value=value, ms=ms, stage_ms=stage_ms, clocks=clock_info, solve_state=state, tile=(tx.value, ty.value),
                 e2e=dict(value=world * cells * e2e_steps / (e2e_ms * 1e-3), unit=METRIC,
                          h2d_bytes_per_step=state_bytes, d2h_bytes_per_step=state_bytes),
                 dt=state.dt)
@@ -294,7 +297,9 @@ def bench_ours(args, world, rank, local):
         compute_frac = flops / peak_tflops
         hbm_frac = gbs / hbm_peak
         bound = "fp64" if key == "f64" else ("fp32" if compute_frac >= hbm_frac else "hbm")
-        out = {"kernel": f"stage_kernel<{'double' if w == 8 else 'float'},ppm4,roe> (RK3 stage 2)",
+        family = "stage_kernel_march" if res["tile"][0] == 58 else "stage_kernel_fast"
+        out = {"kernel": f"{family}<{'double' if w == 8 else 'float'},ppm4,roe,4> (RK3 stage 2, "
+                         f"tile {res['tile'][0]}x{res['tile'][1]})",
                "bound": bound, "achieved": round(flops, 4), "peak": round(peak_tflops, 4),
                "unit": "TFLOP/s", "frac": round(compute_frac, 4),
                "peak_source": f"{key.upper()} FMA pipe measured live by jx_probe_fma",

@@ -16,7 +16,13 @@
 // exception: a product a*b that underflows to +-0 is classified by the signs
 // of a and b); NaN operands are treated as large numbers instead of being
 // skipped by fmin/fmax, which only matters for a state that has already
-// failed. Single precision uses the native instructions.
+// failed. Single precision uses the native instructions, and takes the
+// reciprocals and square roots of the primitive recovery, the Riemann
+// solvers' Roe averages and wave-speed weights and the CFL speeds from the
+// special-function unit's approximations (PTX rcp.approx.f32 and
+// sqrt.approx.f32, at most about one unit in the last place off) instead of
+// the correctly rounded sequences; float64 keeps correctly rounded division
+// and square root.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -62,6 +68,18 @@ template <> struct Num<float> {
   static __device__ __forceinline__ bool lt(float a, float b) { return a < b; }    // a < b
   // max of a >= 0 and b >= 0 or NaN, propagating NaN
   static __device__ __forceinline__ float nanmax_pos(float a, float b) { return (b > a || b != b) ? b : a; }
+  // 1/x, sqrt(x) and a/b from the special-function unit (see above)
+  static __device__ __forceinline__ float rcp(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float root(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
 };
 
 template <> struct Num<double> {
@@ -107,6 +125,9 @@ template <> struct Num<double> {
     const long long x = bits(a) & kMag, y = bits(b) & kMag;
     return y > x ? __longlong_as_double(y) : __longlong_as_double(x);
   }
+  static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+  static __device__ __forceinline__ double root(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
 };
 
 // ---------------------------------------------------------------------------
@@ -301,8 +322,8 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
                                           R& f0, R& f1, R& f2) {
   // fluxes.py:186-201.
   using N = Num<R>;
-  const R sl = sqrt(dl), sr = sqrt(dr);
-  const R u = (sl * ul + sr * ur) * (R(1) / (sl + sr));
+  const R sl = N::root(dl), sr = N::root(dr);
+  const R u = (sl * ul + sr * ur) * N::rcp(sl + sr);
   const R alo = N::min(u - g.cs, ul - g.cs);
   const R ahi = N::max(u + g.cs, ur + g.cs);
   const R bm = N::lt0(alo) ? alo : R(-1e-20);
@@ -310,7 +331,7 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
   const R vl = ul - bm, vr = ur - bp;
   const R fl0 = dl * vl, fl1 = dl * ul * vl + g.cs2 * dl, fl2 = dl * tl * vl;
   const R fr0 = dr * vr, fr1 = dr * ur * vr + g.cs2 * dr, fr2 = dr * tr * vr;
-  const R w = R(0.5) * (bp + bm) / (bp - bm);
+  const R w = N::div(R(0.5) * (bp + bm), bp - bm);
   f0 = R(0.5) * (fl0 + fr0) + w * (fl0 - fr0);
   f1 = R(0.5) * (fl1 + fr1) + w * (fl1 - fr1);
   f2 = R(0.5) * (fl2 + fr2) + w * (fl2 - fr2);
@@ -326,8 +347,8 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
   const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
   const R a0 = R(0.5) * (l0 + r0), a1 = R(0.5) * (l1 + r1), a2 = R(0.5) * (l2 + r2);
-  const R sl = sqrt(dl), sr = sqrt(dr);
-  const R inv = R(1) / (sl + sr);
+  const R sl = N::root(dl), sr = N::root(dr);
+  const R inv = N::rcp(sl + sr);
   const R u = (sl * ul + sr * ur) * inv;
   const R t = (sl * tl + sr * tr) * inv;
   const R lm = u - g.cs, lp = u + g.cs;

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
     const R* u = U + ((size_t)gy * p.nx + gx) * NV;
     R rho = u[0];
     rho = N::lt(rho, k.dfloor) ? k.dfloor : rho;
-    const R inv = R(1) / rho;
+    const R inv = Num<R>::rcp(rho);
     const int s = ly * PW + lx;
     t.W[s] = rho;
     for (int v = 1; v < NV; ++v) t.W[v * t.wplane + s] = inv * u[v];
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
     }
     if (p.want_cfl) {
       // Both candidates are >= cs > 0 or NaN: an ordered max that keeps NaN.
-      const R inv = R(1) / out0;
+      const R inv = Num<R>::rcp(out0);
       vmax0 = N::nanmax_pos(vmax0, fabs(inv * out1) + k.cs);
       vmax1 = N::nanmax_pos(vmax1, fabs(inv * out2) + k.cs);
     }

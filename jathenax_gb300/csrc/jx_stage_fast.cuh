@@ -288,7 +288,7 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
     const Cell4<R> u = load_cell<R, NV>(U + ((size_t)gy * p.nx + gx) * NV);
     Cell4<R> w;
     const R rho = N::lt(u.v[0], k.dfloor) ? k.dfloor : u.v[0];
-    const R inv = R(1) / rho;
+    const R inv = Num<R>::rcp(rho);
     w.v[0] = rho;
 #pragma unroll
     for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? inv * u.v[v] : R(0);
@@ -338,7 +338,7 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
     if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
     store_cell<R, NV>(Uo + cell * NV, un);
     if (p.want_cfl) {
-      const R inv = R(1) / un.v[0];
+      const R inv = Num<R>::rcp(un.v[0]);
       vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
       vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
     }

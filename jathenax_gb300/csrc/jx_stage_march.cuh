@@ -47,7 +47,7 @@ template <typename R, int NV>
 __device__ __forceinline__ Cell4<R> recover_cell(const Cell4<R>& u, R dfloor) {
   Cell4<R> w;
   const R rho = Num<R>::lt(u.v[0], dfloor) ? dfloor : u.v[0];
-  const R inv = R(1) / rho;
+  const R inv = Num<R>::rcp(rho);
   w.v[0] = rho;
 #pragma unroll
   for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? inv * u.v[v] : R(0);
@@ -311,7 +311,7 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
           if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
           store_cell<R, NV>(Uo + cell * NV, un);
           if (p.want_cfl) {
-            const R inv = R(1) / un.v[0];
+            const R inv = Num<R>::rcp(un.v[0]);
             vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
             vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
           }
