@@ -40,7 +40,9 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # ncu-measured DRAM bytes per cell for one launch of the fused stage kernel
 # (stage 2 of RK3, ppm4+roe, 4 variables), from the capture summarised in
 # profiles/; None until such a capture exists for the dtype.
-STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": 377.4e6 / 2048**2, "f32": 175.1e6 / 2048**2}
+# DRAM bytes (read + write) of one RK3 stage-2 launch at 4096^2, from a one-pass
+# ncu capture of this benchmark (dram__bytes_read.sum + dram__bytes_write.sum).
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1.08e9 + 510.69e6) / 4096**2, "f32": (597.40e6 + 238.46e6) / 4096**2}
 
 
 def parse_args():

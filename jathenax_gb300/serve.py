@@ -65,19 +65,27 @@ def make_stream(n, rate, seed=0, side_range=(64, 2048), tlim_range=(0.2, 3.0), f
     return out
 
 
-def build_solve(req, tile=(0, 0), clock=None, dtype=None):
+# Stage tiles of a served request by precision: float32 marches over 58 x 16
+# tiles (short enough that a batch of small grids keeps every SM busy; the
+# single-solve default picks taller tiles for a whole GPU), float64 uses the
+# 32 x 16 shared-memory tile.
+SERVING_TILES = {"float32": (58, 16), "float64": (32, 16)}
+
+
+def build_solve(req, tile=None, clock=None, dtype=None):
     """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163).
 
-    ``tile`` (0, 0) is the library default: marching tiles in float32,
-    shared-memory tiles in float64.
+    ``tile`` None picks :data:`SERVING_TILES` by precision.
     """
     t = _lib.torch()
     from .forcing import cartesian_modes, forcing_basis, modal_coefficients
     from .initial_conditions import cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest
     from .solver import Solve
     n = req.side
-    kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver, tile=tuple(tile),
-              dtype=getattr(t, dtype or req.dtype), clock=clock)
+    dtype = dtype or req.dtype
+    kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver,
+              tile=tuple(tile) if tile is not None else SERVING_TILES[dtype],
+              dtype=getattr(t, dtype), clock=clock)
     if req.problem == "kh":
         return Solve(kelvin_helmholtz_tanh(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
     if req.problem == "smooth":
@@ -109,10 +117,10 @@ def footprint_bytes(req, dtype=None):
 class Server:
     """Continuous-batching request loop with an HBM admission budget."""
 
-    def __init__(self, budget_bytes=150e9, tile=(0, 0), steps_per_tick=4, blocks_per_sm=0,
+    def __init__(self, budget_bytes=150e9, tile=None, steps_per_tick=4, blocks_per_sm=0,
                  max_live=1024, keep_results=False, dtype=None, builder=None):
         self.budget = float(budget_bytes)
-        self.tile = tuple(tile)
+        self.tile = tile  # None: SERVING_TILES by precision
         self.steps_per_tick = steps_per_tick
         self.blocks_per_sm = blocks_per_sm
         self.max_live = max_live
