@@ -190,8 +190,19 @@ def to_device(x, dtype=None):
     arr = np.asarray(x)
     if dtype is None and arr.dtype not in (np.float32, np.float64):
         arr = arr.astype(np.float64)
-    out = t.from_numpy(np.ascontiguousarray(arr)).to(device())
+    out = _upload(np.ascontiguousarray(arr))
     return out.to(dtype) if dtype is not None else out
+
+
+def _upload(arr):
+    """Host array -> new device tensor, stream-ordered: staged in pinned memory
+    (torch's host allocator keeps the staging block until the copy is done),
+    so the caller does not wait for work already queued on the GPU."""
+    t = torch()
+    host = t.from_numpy(arr)
+    if host.numel() == 0:
+        return host.to(device())
+    return host.pin_memory().to(device(), non_blocking=True)
 
 
 def like_input(tensor, template):
@@ -209,7 +220,7 @@ def new_clock(**fields):
     for key, value in fields.items():
         setattr(c, key, value)
     host = np.frombuffer(bytes(c), dtype=np.uint8).copy()
-    return torch().from_numpy(host).to(device())
+    return _upload(host)
 
 
 def read_clock(tensor):

@@ -1,12 +1,14 @@
 """Batches: many independent device-resident solves advanced together.
 
 Per RK stage, one persistent launch per (precision, reconstruction, Riemann
-solver) group walks a tile work list spanning every grid of the group; the
-batched begin-step kernel picks each solve's own dt; forced solves get their
-own render/normalise/kick launches. A whole cycle is enqueued by one
-``jx_batch_step`` call and can be captured in a CUDA graph. Each solve keeps
-its own clock, workspace and CFL partials (one slot per tile), so a solve's
-result is bitwise the same alone and in any batch.
+solver, kernel) group walks a tile work list spanning every grid of the
+group, the groups of a stage running concurrently on side streams; the
+batched begin-step kernel picks each solve's own dt; the forced solves of
+one precision share one render launch and one normalise/kick sequence. A
+whole cycle is enqueued by one ``jx_batch_step`` call and can be captured in
+a CUDA graph. Each solve keeps its own clock, workspace and CFL partials
+(one slot per tile), so a solve's result is bitwise the same alone and in
+any batch.
 """
 
 import ctypes
@@ -20,12 +22,36 @@ class ClockBank:
     def __init__(self, n):
         t = _lib.torch()
         self.buf = t.zeros((n, 128), dtype=t.uint8, device=_lib.device())
+        self._host = None
+        self._turn = 0
 
     def slot(self, i):
         return self.buf[i]
 
     def read(self):
-        raw = self.buf.cpu().numpy()
+        """Every clock, now (synchronises with the device)."""
+        return self.parse(self.buf.cpu())
+
+    def snapshot(self):
+        """Enqueue a copy of every clock into pinned host memory.
+
+        Returns (event, host): once the event has completed, ``parse(host)``
+        gives the clocks as of this point of the stream. Two host buffers
+        alternate, so a snapshot stays readable while the next one is copied.
+        """
+        t = _lib.torch()
+        if self._host is None:
+            self._host = [t.empty(self.buf.shape, dtype=t.uint8).pin_memory() for _ in range(2)]
+        host = self._host[self._turn]
+        self._turn ^= 1
+        host.copy_(self.buf, non_blocking=True)
+        event = t.cuda.Event(enable_timing=True)
+        event.record()
+        return event, host
+
+    @staticmethod
+    def parse(host):
+        raw = host.numpy()
         return [_lib.Clock.from_buffer_copy(raw[i].tobytes()) for i in range(raw.shape[0])]
 
 
@@ -33,7 +59,7 @@ class Batch:
     """Advance a list of :class:`jathenax_gb300.solver.Solve` together.
 
     Solves have 3 or 4 variables; each keeps its own tile (the default, or
-    ``tile=(32, h)`` / ``tile=(104, h)`` at construction).
+    ``tile=(32, h)`` / ``tile=(58, h)`` at construction).
     """
 
     def __init__(self, solves, blocks_per_sm=0, clocks=None, plan_buffers=None):

@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "jx_aux.cuh"
@@ -382,10 +383,8 @@ jx_status do_stage(const jx_desc* d, const Tile& t, const Ws& w, int stage, cons
   return cuda_check(launch_stage(d, p, t, s), "stage kernel");
 }
 
-jx_status do_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock,
-                  const jx_trace* trace, const Ws& w, cudaStream_t s) {
-  if (!f || !f->raw_force) return fail(JX_ERR_INVALID, "forcing needs a raw_force buffer");
-  if (!U || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
+ForceParams force_params(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock, const jx_trace* trace,
+                         const Ws& w) {
   ForceParams q;
   memset(&q, 0, sizeof(q));
   q.clock = clock;
@@ -409,7 +408,31 @@ jx_status do_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* cloc
   q.want_cfl = !(d->smagorinsky_cs > 0.0);
   q.dfloor = d->dfloor;
   q.cs = d->cs;
-  return cuda_check(launch_force_kick(d->dtype, q, s), "force kick kernels");
+  return q;
+}
+
+RenderParams render_params(const jx_desc* d, const jx_forcing* f, jx_clock* clock) {
+  RenderParams q;
+  memset(&q, 0, sizeof(q));
+  q.clock = clock;
+  q.table = f->table;
+  q.cos_x = f->cos_x;
+  q.sin_x = f->sin_x;
+  q.cos_y = f->cos_y;
+  q.sin_y = f->sin_y;
+  q.raw = f->raw_force;
+  q.ny = d->ny;
+  q.nx = d->nx;
+  q.n_modes = f->n_modes;
+  q.n_updates = f->n_updates;
+  return q;
+}
+
+jx_status do_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock,
+                  const jx_trace* trace, const Ws& w, cudaStream_t s) {
+  if (!f || !f->raw_force) return fail(JX_ERR_INVALID, "forcing needs a raw_force buffer");
+  if (!U || !clock) return fail(JX_ERR_INVALID, "null state or clock pointer");
+  return cuda_check(launch_force_kick(d->dtype, force_params(d, f, U, clock, trace, w), s), "force kick kernels");
 }
 
 }  // namespace
@@ -514,19 +537,7 @@ jx_status jx_force_render(const jx_desc* d, const jx_forcing* f, jx_clock* clock
   if (!f || !clock || !f->table || !f->cos_x || !f->sin_x || !f->cos_y || !f->sin_y || !f->raw_force)
     return fail(JX_ERR_INVALID, "incomplete forcing tables");
   if (f->n_modes < 1 || f->n_updates < 1) return fail(JX_ERR_INVALID, "forcing needs modes and updates");
-  RenderParams q;
-  q.clock = clock;
-  q.table = f->table;
-  q.cos_x = f->cos_x;
-  q.sin_x = f->sin_x;
-  q.cos_y = f->cos_y;
-  q.sin_y = f->sin_y;
-  q.raw = f->raw_force;
-  q.ny = d->ny;
-  q.nx = d->nx;
-  q.n_modes = f->n_modes;
-  q.n_updates = f->n_updates;
-  return cuda_check(launch_render(d->dtype, q, (cudaStream_t)s), "render kernel");
+  return cuda_check(launch_render(d->dtype, render_params(d, f, clock), (cudaStream_t)s), "render kernel");
 }
 
 jx_status jx_force_kick(const jx_desc* d, const jx_forcing* f, void* U, jx_clock* clock,
@@ -665,7 +676,8 @@ constexpr int kMaxGroups = 90;  // 2 precisions x 5 reconstructions x 3 solvers 
 
 struct BatchGroup {
   int dtype, recon, rsolver, first, count, tile_first, nwork, march;
-  int nv, pad;  // marching groups: the variable count of every solve (0 in shared-memory groups)
+  int nv;   // marching groups: the variable count of every solve (0 in shared-memory groups)
+  int bps;  // resident blocks per SM of the group's kernel (occupancy at plan time)
   size_t smem;
 };
 
@@ -674,15 +686,26 @@ struct BatchSolveInfo {
   int forced, smag, n_stages, pad;
 };
 
+// Forced solves of one precision: their render and kick parameters sit at
+// [first, first + count) of the plan's force arrays; block offsets of the
+// render, the two sum passes and the kick at [off, off + count + 1) of the
+// three offset arrays.
+struct ForceGroup {
+  int dtype, first, count, off;
+  int render_work, sum_work, kick_work, pad;
+};
+
 struct BatchPlanHeader {
   uint32_t magic;
-  int32_t n, n_groups, max_stages, pad;
+  int32_t n, n_groups, max_stages, n_force_groups;
   int64_t bytes, off_params, off_offsets, off_begin, off_info;
+  int64_t off_force, off_render, off_force_offsets;
   BatchGroup groups[kMaxGroups];
+  ForceGroup force_groups[2];
 };
 
 struct PlanLayout {
-  size_t params, offsets, begin, info, total;
+  size_t params, offsets, begin, info, force, render, force_offsets, total;
 };
 
 PlanLayout plan_layout(int n) {
@@ -696,6 +719,12 @@ PlanLayout plan_layout(int n) {
   off = align256(off + (size_t)n * sizeof(BeginParams));
   L.info = off;
   off = align256(off + (size_t)n * sizeof(BatchSolveInfo));
+  L.force = off;
+  off = align256(off + (size_t)n * sizeof(ForceParams));
+  L.render = off;
+  off = align256(off + (size_t)n * sizeof(RenderParams));
+  L.force_offsets = off;
+  off = align256(off + (size_t)3 * (n + 2) * sizeof(int));
   L.total = off;
   return L;
 }
@@ -755,6 +784,38 @@ cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, const 
   }
 }
 
+// Side streams of one device for the concurrent stage groups of a batch step;
+// the returned lock serialises batch steps of different host threads on them
+// (the fork and join events are shared).
+constexpr int kSideStreams = 8;
+
+struct SideStreams {
+  cudaStream_t s[kSideStreams];
+  cudaEvent_t fork, join[kSideStreams];
+  bool ready;
+};
+
+std::mutex g_side_mutex[64];
+SideStreams g_side[64];
+
+jx_status side_streams(SideStreams** out, std::unique_lock<std::mutex>* lock) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(JX_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(JX_ERR_INVALID, "device ordinal %d out of range", dev);
+  *lock = std::unique_lock<std::mutex>(g_side_mutex[dev]);
+  SideStreams& S = g_side[dev];
+  if (!S.ready) {
+    for (int k = 0; k < kSideStreams && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&S.s[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming);
+    for (int k = 0; k < kSideStreams && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&S.join[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(JX_ERR_CUDA, "side streams: %s", cudaGetErrorString(e));
+    S.ready = true;
+  }
+  *out = &S;
+  return JX_OK;
+}
+
 jx_status check_batch_solve(int i, const jx_solve& in, Tile* t, Ws* w) {
   jx_status st = check_desc(&in.desc);
   if (st) return fail(st, "solve %d: %s", i, jx_last_error());
@@ -802,6 +863,9 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
   h->off_offsets = (int64_t)L.offsets;
   h->off_begin = (int64_t)L.begin;
   h->off_info = (int64_t)L.info;
+  h->off_force = (int64_t)L.force;
+  h->off_render = (int64_t)L.render;
+  h->off_force_offsets = (int64_t)L.force_offsets;
   StageParams* params = reinterpret_cast<StageParams*>(base + L.params);
   int* offsets = reinterpret_cast<int*>(base + L.offsets);
   BeginParams* begin = reinterpret_cast<BeginParams*>(base + L.begin);
@@ -894,6 +958,58 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
     G.nwork = tiles;
   }
   h->n_groups = n_groups;
+  for (int g = 0; g < n_groups; ++g) {
+    BatchGroup& G = h->groups[g];
+    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv)
+                    : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
+    if (G.bps < 1) {
+      cudaGetLastError();  // no device to query: one block per SM
+      G.bps = 1;
+    }
+  }
+
+  // Forced solves, grouped by precision, for the batched render and kick.
+  ForceParams* fq = reinterpret_cast<ForceParams*>(base + L.force);
+  RenderParams* rq = reinterpret_cast<RenderParams*>(base + L.render);
+  int* foff = reinterpret_cast<int*>(base + L.force_offsets);
+  int* off_render = foff;
+  int* off_sum = foff + (n + 2);
+  int* off_kick = foff + 2 * (n + 2);
+  int nf = 0, next_off = 0;
+  for (int dt = JX_F64; dt <= JX_F32; ++dt) {
+    ForceGroup F;
+    memset(&F, 0, sizeof(F));
+    F.dtype = dt;
+    F.first = nf;
+    F.off = next_off;
+    for (int k = 0; k < n; ++k) {
+      const BatchSolveInfo& I = info[k];
+      if (!I.forced || I.solve.desc.dtype != dt) continue;
+      const jx_desc& d = I.solve.desc;
+      Tile t;
+      Ws w;
+      if ((st = resolve_tile(&d, &t)) || (st = bind_ws(&d, t, I.solve.workspace, I.solve.workspace_bytes, &w)))
+        return st;
+      fq[nf] = force_params(&d, &I.solve.forcing, I.solve.S, I.solve.clock, nullptr, w);
+      rq[nf] = render_params(&d, &I.solve.forcing, I.solve.clock);
+      const int64_t ncell = (int64_t)d.ny * d.nx;
+      off_render[next_off] = F.render_work;
+      off_sum[next_off] = F.sum_work;
+      off_kick[next_off] = F.kick_work;
+      F.render_work += render_blocks(ncell);
+      F.sum_work += fq[nf].nblk;
+      F.kick_work += cfl_grid(ncell);
+      ++next_off;
+      ++nf;
+      ++F.count;
+    }
+    if (F.count == 0) continue;
+    off_render[next_off] = F.render_work;
+    off_sum[next_off] = F.sum_work;
+    off_kick[next_off] = F.kick_work;
+    ++next_off;
+    h->force_groups[h->n_force_groups++] = F;
+  }
   return JX_OK;
 }
 
@@ -909,18 +1025,35 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
   const BeginParams* begin_dev = reinterpret_cast<const BeginParams*>(dbase + h->off_begin);
   jx_status st;
   if ((st = cuda_check(launch_begin_step_batch(begin_dev, h->n, s), "batched begin-step kernel"))) return st;
-  for (int i = 0; i < h->n; ++i)
-    if (info[i].forced && (st = jx_force_render(&info[i].solve.desc, &info[i].solve.forcing, info[i].solve.clock,
-                                                stream)))
+  const ForceParams* force_dev = reinterpret_cast<const ForceParams*>(dbase + h->off_force);
+  const RenderParams* render_dev = reinterpret_cast<const RenderParams*>(dbase + h->off_render);
+  const int* foff_dev = reinterpret_cast<const int*>(dbase + h->off_force_offsets);
+  for (int g = 0; g < h->n_force_groups; ++g) {
+    const ForceGroup& F = h->force_groups[g];
+    if ((st = cuda_check(launch_render_batch(F.dtype, render_dev + F.first, foff_dev + F.off, F.count,
+                                             F.render_work, s),
+                         "batched render kernel")))
       return st;
+  }
+  // A stage's launch groups are independent (disjoint solves): with more
+  // than one they run concurrently on side streams that fork from and join
+  // back to the caller's stream around each stage (also inside a graph
+  // capture), so small groups do not wait for one another.
   const int sms = sm_count();
+  SideStreams* side = nullptr;
+  std::unique_lock<std::mutex> side_lock;
+  if (h->n_groups > 1 && (st = side_streams(&side, &side_lock))) return st;
   for (int stage = 1; stage <= h->max_stages; ++stage) {
+    const int used = side ? (h->n_groups < kSideStreams ? h->n_groups : kSideStreams) : 0;
+    if (side) {
+      if ((st = cuda_check(cudaEventRecord(side->fork, s), "fork event"))) return st;
+      for (int k = 0; k < used; ++k)
+        if ((st = cuda_check(cudaStreamWaitEvent(side->s[k], side->fork, 0), "side stream wait"))) return st;
+    }
     for (int g = 0; g < h->n_groups; ++g) {
       const BatchGroup& G = h->groups[g];
       int bps = blocks_per_sm;
-      if (bps <= 0)
-        bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv)
-                      : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
+      if (bps <= 0) bps = G.bps;
       if (bps < 1) bps = 1;
       int64_t blocks = (int64_t)sms * bps;
       const int64_t per_block = G.march ? kMarchWarps : 1;  // marching blocks take one tile per warp
@@ -928,26 +1061,37 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
       if (blocks < 1) continue;
       const StageParams* P = params_dev + (size_t)(stage - 1) * h->n + G.first;
       const int* offs = offsets_dev + G.tile_first;
+      cudaStream_t gs = side ? side->s[g % kSideStreams] : s;
       const cudaError_t e =
           G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, P, offs, G.count, G.nwork,
-                                       dim3((unsigned)blocks), s)
+                                       dim3((unsigned)blocks), gs)
                   : launch_batch(G.recon, G.dtype, G.rsolver, P, offs, G.count, G.nwork, dim3((unsigned)blocks),
-                                 G.smem, s);
+                                 G.smem, gs);
       if ((st = cuda_check(e, "batched stage kernel"))) return st;
     }
+    for (int k = 0; k < used; ++k) {
+      if ((st = cuda_check(cudaEventRecord(side->join[k], side->s[k]), "join event"))) return st;
+      if ((st = cuda_check(cudaStreamWaitEvent(s, side->join[k], 0), "join wait"))) return st;
+    }
+  }
+  for (int g = 0; g < h->n_force_groups; ++g) {
+    const ForceGroup& F = h->force_groups[g];
+    const int* off_sum = foff_dev + (h->n + 2) + F.off;
+    const int* off_kick = foff_dev + 2 * (h->n + 2) + F.off;
+    if ((st = cuda_check(launch_force_kick_batch(F.dtype, force_dev + F.first, F.count, off_sum, F.sum_work, off_kick,
+                                                 F.kick_work, s),
+                         "batched force kick kernels")))
+      return st;
   }
   for (int i = 0; i < h->n; ++i) {
     const jx_solve& sv = info[i].solve;
-    if (!info[i].forced && !info[i].smag) continue;
+    if (!info[i].smag) continue;
     Tile t;
     Ws w;
     if ((st = resolve_tile(&sv.desc, &t)) || (st = bind_ws(&sv.desc, t, sv.workspace, sv.workspace_bytes, &w)))
       return st;
-    if (info[i].forced && (st = do_kick(&sv.desc, &sv.forcing, sv.S, sv.clock, nullptr, w, s))) return st;
-    if (info[i].smag) {
-      CflParams q = cfl_params(&sv.desc, sv.S, sv.clock, w);
-      if ((st = cuda_check(launch_cfl(sv.desc.dtype, false, q, s), "cfl kernel"))) return st;
-    }
+    CflParams q = cfl_params(&sv.desc, sv.S, sv.clock, w);
+    if ((st = cuda_check(launch_cfl(sv.desc.dtype, false, q, s), "cfl kernel"))) return st;
   }
   return JX_OK;
 }
@@ -973,8 +1117,6 @@ int32_t jx_batch_groups(const void* plan) {
 // but two calls whose kernels overlap on the GPU (different streams, or
 // different host threads) race on the array.
 // ---------------------------------------------------------------------------
-#include <mutex>
-
 namespace {
 
 constexpr size_t kNoAllocSlots = jx::kCflBlocksMax;

@@ -190,11 +190,16 @@ __global__ void cfl_kernel(CflParams q) {
 // ---------------------------------------------------------------------------
 // Forcing: render (forcing.py:111-122), normalise (forcing.py:137-149), kick.
 // ---------------------------------------------------------------------------
+// Each forcing kernel is a per-block body taking the block's index b within
+// its solve and the solve's block count nb; the single-solve kernels pass
+// blockIdx.x and gridDim.x, the batched kernels (one launch for every forced
+// solve of a batch) the position of the block in the solve's own range, so a
+// solve's sums are bitwise the same alone and in a batch.
 template <typename R>
-__global__ void render_kernel(RenderParams q) {
+__device__ __forceinline__ void render_body(const RenderParams& q, int b) {
   if (q.clock->done || !q.clock->render) return;
   const int64_t n = (int64_t)q.ny * q.nx;
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = (int64_t)b * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int j = (int)(k / q.nx), i = (int)(k - (int64_t)j * q.nx);
   const R* cx = static_cast<const R*>(q.cos_x);
@@ -206,10 +211,10 @@ __global__ void render_kernel(RenderParams q) {
   const double* amp = q.table + (size_t)(valid ? row : 0) * q.n_modes * 4;
   R f0 = R(0), f1 = R(0);
   for (int m = 0; m < q.n_modes; ++m) {
-    const R a = cx[(size_t)m * q.nx + i], b = sx[(size_t)m * q.nx + i];
+    const R a = cx[(size_t)m * q.nx + i], b2 = sx[(size_t)m * q.nx + i];
     const R c = cy[(size_t)m * q.ny + j], d = sy[(size_t)m * q.ny + j];
-    const R re = a * c - b * d;
-    const R im = a * d + b * c;
+    const R re = a * c - b2 * d;
+    const R im = a * d + b2 * c;
     R a00 = static_cast<R>(amp[m * 4 + 0]), a01 = static_cast<R>(amp[m * 4 + 1]);
     R a10 = static_cast<R>(amp[m * 4 + 2]), a11 = static_cast<R>(amp[m * 4 + 3]);
     if (!valid) a00 = a01 = a10 = a11 = static_cast<R>(NAN);
@@ -223,13 +228,12 @@ __global__ void render_kernel(RenderParams q) {
 
 // Pass 1: block partials of sum(rho), sum(rho*Fx), sum(rho*Fy).
 template <typename R>
-__global__ void force_sum1_kernel(ForceParams q) {
+__device__ __forceinline__ void sum1_body(const ForceParams& q, int b, double* red) {
   if (q.clock->done) return;
-  __shared__ double red[32 * 3];
   const R* U = static_cast<const R*>(q.U);
   const R* F = static_cast<const R*>(q.raw);
   const int64_t n = (int64_t)q.ny * q.nx;
-  const int64_t lo = (int64_t)blockIdx.x * q.chunk, hi = min(n, lo + q.chunk);
+  const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
   double v[3] = {0.0, 0.0, 0.0};
   for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
     const R rho = U[k * q.nv];
@@ -239,7 +243,7 @@ __global__ void force_sum1_kernel(ForceParams q) {
   }
   block_sum<3>(v, red);
   if (threadIdx.x == 0) {
-    double* out = q.p1 + (size_t)blockIdx.x * 4;
+    double* out = q.p1 + (size_t)b * 4;
     out[0] = v[0];
     out[1] = v[1];
     out[2] = v[2];
@@ -247,9 +251,8 @@ __global__ void force_sum1_kernel(ForceParams q) {
 }
 
 // Finish pass 1: the mass-weighted mean acceleration.
-__global__ void force_fin1_kernel(ForceParams q) {
+__device__ __forceinline__ void fin1_body(const ForceParams& q, double* red) {
   if (q.clock->done) return;
-  __shared__ double red[32 * 3];
   double v[3] = {0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < q.nblk; b += blockDim.x) {
     v[0] += q.p1[b * 4 + 0];
@@ -265,15 +268,14 @@ __global__ void force_fin1_kernel(ForceParams q) {
 
 // Pass 2: partials of sum(0.5 rho |F - mean|^2 dt) and sum(m . (F - mean)).
 template <typename R>
-__global__ void force_sum2_kernel(ForceParams q) {
+__device__ __forceinline__ void sum2_body(const ForceParams& q, int b, double* red) {
   if (q.clock->done) return;
-  __shared__ double red[32 * 2];
   const R* U = static_cast<const R*>(q.U);
   const R* F = static_cast<const R*>(q.raw);
   const R mx = static_cast<R>(q.scal[0]), my = static_cast<R>(q.scal[1]);
   const R dt = static_cast<R>(q.clock->dt);
   const int64_t n = (int64_t)q.ny * q.nx;
-  const int64_t lo = (int64_t)blockIdx.x * q.chunk, hi = min(n, lo + q.chunk);
+  const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
   double v[2] = {0.0, 0.0};
   for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
     const R* u = U + k * q.nv;
@@ -284,15 +286,14 @@ __global__ void force_sum2_kernel(ForceParams q) {
   }
   block_sum<2>(v, red);
   if (threadIdx.x == 0) {
-    q.p2[(size_t)blockIdx.x * 4 + 0] = v[0];
-    q.p2[(size_t)blockIdx.x * 4 + 1] = v[1];
+    q.p2[(size_t)b * 4 + 0] = v[0];
+    q.p2[(size_t)b * 4 + 1] = v[1];
   }
 }
 
 // Finish pass 2: the edot quadratic solve for the amplitude scale.
-__global__ void force_fin2_kernel(ForceParams q) {
+__device__ __forceinline__ void fin2_body(const ForceParams& q, double* red) {
   if (q.clock->done) return;
-  __shared__ double red[32 * 2];
   double v[2] = {0.0, 0.0};
   for (int b = threadIdx.x; b < q.nblk; b += blockDim.x) {
     v[0] += q.p2[b * 4 + 0];
@@ -312,11 +313,11 @@ __global__ void force_fin2_kernel(ForceParams q) {
   }
 }
 
-// Kick (hydro.py:128-132), density floor (hydro.py:143), CFL partials.
+// Kick (hydro.py:128-132), density floor (hydro.py:143), CFL partials;
+// block b of nb strides over the solve's cells.
 template <typename R>
-__global__ void force_kick_kernel(ForceParams q) {
+__device__ __forceinline__ void kick_body(const ForceParams& q, int b, int nb, double* red) {
   if (q.clock->done) return;
-  __shared__ double red[32 * 2];
   R* U = static_cast<R*>(q.Uw);
   const R* F = static_cast<const R*>(q.raw);
   const double power = q.clock->power;
@@ -329,8 +330,7 @@ __global__ void force_kick_kernel(ForceParams q) {
   R* after = static_cast<R*>(q.conserved);
   const int64_t n = (int64_t)q.ny * q.nx;
   double v[2] = {0.0, 0.0};
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t k = (int64_t)b * blockDim.x + threadIdx.x; k < n; k += (int64_t)nb * blockDim.x) {
     R* u = U + k * q.nv;
     if (before)
       for (int c = 0; c < q.nv; ++c) before[k * q.nv + c] = u[c];
@@ -357,7 +357,7 @@ __global__ void force_kick_kernel(ForceParams q) {
     u[1] = m1;
     u[2] = m2;
     if (q.want_cfl) {
-      const R inv = R(1) / rf;
+      const R inv = Num<R>::rcp(rf);
       v[0] = nan_max(v[0], static_cast<double>(fabs(inv * m1) + cs));
       v[1] = nan_max(v[1], static_cast<double>(fabs(inv * m2) + cs));
     }
@@ -365,13 +365,95 @@ __global__ void force_kick_kernel(ForceParams q) {
   if (q.want_cfl) {
     block_nan_max<2>(v, red);
     if (threadIdx.x == 0) {
-      double* out = q.partials + (size_t)blockIdx.x * kCflSlots;
+      double* out = q.partials + (size_t)b * kCflSlots;
       out[0] = v[0];
       out[1] = v[1];
       out[2] = 0.0;
-      if (blockIdx.x == 0) q.header->n_cfl = gridDim.x;
+      if (b == 0) q.header->n_cfl = nb;
     }
   }
+}
+
+template <typename R>
+__global__ void render_kernel(RenderParams q) {
+  render_body<R>(q, blockIdx.x);
+}
+
+template <typename R>
+__global__ void force_sum1_kernel(ForceParams q) {
+  __shared__ double red[32 * 3];
+  sum1_body<R>(q, blockIdx.x, red);
+}
+
+__global__ void force_fin1_kernel(ForceParams q) {
+  __shared__ double red[32 * 3];
+  fin1_body(q, red);
+}
+
+template <typename R>
+__global__ void force_sum2_kernel(ForceParams q) {
+  __shared__ double red[32 * 2];
+  sum2_body<R>(q, blockIdx.x, red);
+}
+
+__global__ void force_fin2_kernel(ForceParams q) {
+  __shared__ double red[32 * 2];
+  fin2_body(q, red);
+}
+
+template <typename R>
+__global__ void force_kick_kernel(ForceParams q) {
+  __shared__ double red[32 * 2];
+  kick_body<R>(q, blockIdx.x, gridDim.x, red);
+}
+
+// Batched forcing: block w of a launch is block w - off[i] of forced solve i
+// (off[i] <= w < off[i+1]); the finishers take one block per solve.
+__device__ __forceinline__ int batch_solve_of(const int* __restrict__ off, int n, int w) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename R>
+__global__ void render_batch_kernel(const RenderParams* __restrict__ q, const int* __restrict__ off, int n) {
+  const int i = batch_solve_of(off, n, blockIdx.x);
+  render_body<R>(q[i], blockIdx.x - off[i]);
+}
+
+template <typename R>
+__global__ void force_sum1_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
+  __shared__ double red[32 * 3];
+  const int i = batch_solve_of(off, n, blockIdx.x);
+  sum1_body<R>(q[i], blockIdx.x - off[i], red);
+}
+
+__global__ void force_fin1_batch_kernel(const ForceParams* __restrict__ q) {
+  __shared__ double red[32 * 3];
+  fin1_body(q[blockIdx.x], red);
+}
+
+template <typename R>
+__global__ void force_sum2_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
+  __shared__ double red[32 * 2];
+  const int i = batch_solve_of(off, n, blockIdx.x);
+  sum2_body<R>(q[i], blockIdx.x - off[i], red);
+}
+
+__global__ void force_fin2_batch_kernel(const ForceParams* __restrict__ q) {
+  __shared__ double red[32 * 2];
+  fin2_body(q[blockIdx.x], red);
+}
+
+template <typename R>
+__global__ void force_kick_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
+  __shared__ double red[32 * 2];
+  const int i = batch_solve_of(off, n, blockIdx.x);
+  kick_body<R>(q[i], blockIdx.x - off[i], off[i + 1] - off[i], red);
 }
 
 // ---------------------------------------------------------------------------
@@ -629,8 +711,7 @@ cudaError_t launch_cfl(int dtype, bool from_w, const CflParams& q, cudaStream_t 
 }
 
 cudaError_t launch_render(int dtype, const RenderParams& q, cudaStream_t s) {
-  const int64_t n = (int64_t)q.ny * q.nx;
-  const int g = (int)((n + kReduceThreads - 1) / kReduceThreads);
+  const int g = render_blocks((int64_t)q.ny * q.nx);
   if (dtype == JX_F64) render_kernel<double><<<g, kReduceThreads, 0, s>>>(q);
   else render_kernel<float><<<g, kReduceThreads, 0, s>>>(q);
   return cudaGetLastError();
@@ -654,6 +735,29 @@ cudaError_t launch_force_kick(int dtype, const ForceParams& q, cudaStream_t s) {
   force_fin2_kernel<<<1, kReduceThreads, 0, s>>>(q);
   if (dtype == JX_F64) force_kick_kernel<double><<<g, kReduceThreads, 0, s>>>(q);
   else force_kick_kernel<float><<<g, kReduceThreads, 0, s>>>(q);
+  return cudaGetLastError();
+}
+
+int render_blocks(int64_t ncell) { return (int)((ncell + kReduceThreads - 1) / kReduceThreads); }
+
+cudaError_t launch_render_batch(int dtype, const RenderParams* q, const int* off, int n, int nwork, cudaStream_t s) {
+  if (n < 1 || nwork < 1) return cudaSuccess;
+  if (dtype == JX_F64) render_batch_kernel<double><<<nwork, kReduceThreads, 0, s>>>(q, off, n);
+  else render_batch_kernel<float><<<nwork, kReduceThreads, 0, s>>>(q, off, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_kick_batch(int dtype, const ForceParams* q, int n, const int* off_sum, int sum_work,
+                                    const int* off_kick, int kick_work, cudaStream_t s) {
+  if (n < 1) return cudaSuccess;
+  if (dtype == JX_F64) force_sum1_batch_kernel<double><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  else force_sum1_batch_kernel<float><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  force_fin1_batch_kernel<<<n, kReduceThreads, 0, s>>>(q);
+  if (dtype == JX_F64) force_sum2_batch_kernel<double><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  else force_sum2_batch_kernel<float><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  force_fin2_batch_kernel<<<n, kReduceThreads, 0, s>>>(q);
+  if (dtype == JX_F64) force_kick_batch_kernel<double><<<kick_work, kReduceThreads, 0, s>>>(q, off_kick, n);
+  else force_kick_batch_kernel<float><<<kick_work, kReduceThreads, 0, s>>>(q, off_kick, n);
   return cudaGetLastError();
 }
 

@@ -161,8 +161,7 @@ def forcing_basis(modes, x, y, lengths, dtype=None):
     py = k[:, 1, None] * y
     t = _lib.torch()
     tdtype = t.float64 if dtype is None else dtype
-    return tuple(t.from_numpy(np.ascontiguousarray(a)).to(_lib.device(), tdtype)
-                 for a in (np.cos(px), np.sin(px), np.cos(py), np.sin(py)))
+    return tuple(_lib.to_device(a, tdtype) for a in (np.cos(px), np.sin(px), np.cos(py), np.sin(py)))
 
 
 def _device_tables(coefficients, basis, dtype):

@@ -15,6 +15,7 @@ The reported metrics are time-to-solution (completion minus arrival:
 queueing + compute) percentiles and solves per second.
 """
 
+import ctypes
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -72,6 +73,27 @@ def make_stream(n, rate, seed=0, side_range=(64, 2048), tlim_range=(0.2, 3.0), f
 SERVING_TILES = {"float32": (58, 16), "float64": (32, 16)}
 
 
+def _device_state(problem, n):
+    """The request's initial state built on the device in float64 (the
+    formulas of initial_conditions.kelvin_helmholtz_tanh, smooth_waves and
+    uniform_rest, evaluated by torch instead of NumPy)."""
+    t = _lib.torch()
+    dev = _lib.device()
+    c = (t.arange(n, dtype=t.float64, device=dev) + 0.5) / n - 0.5
+    Y, X = t.meshgrid(c, c, indexing="ij")
+    if problem == "kh":
+        inside = 0.5 * (t.tanh((Y + 0.25) / 0.01) - t.tanh((Y - 0.25) / 0.01))
+        vy = 0.01 * t.sin(4 * t.pi * X) * (t.exp(-((Y - 0.25) / 0.05) ** 2) + t.exp(-((Y + 0.25) / 0.05) ** 2))
+        return t.stack((t.ones_like(X), inside - 0.5, vy, inside), dim=-1)
+    if problem == "smooth":
+        px, py = 2.0 * t.pi * X, 2.0 * t.pi * Y
+        rho = 1.0 + 0.1 * t.sin(px + py)
+        return t.stack((rho, rho * (0.2 * t.cos(py)), rho * (0.2 * t.sin(px))), dim=-1)
+    U = t.zeros((n, n, 3), dtype=t.float64, device=dev)
+    U[..., 0] = 1.0
+    return U
+
+
 def build_solve(req, tile=None, clock=None, dtype=None):
     """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163).
 
@@ -79,23 +101,24 @@ def build_solve(req, tile=None, clock=None, dtype=None):
     """
     t = _lib.torch()
     from .forcing import cartesian_modes, forcing_basis, modal_coefficients
-    from .initial_conditions import cell_centers, kelvin_helmholtz_tanh, smooth_waves, uniform_rest
+    from .initial_conditions import cell_centers
     from .solver import Solve
     n = req.side
     dtype = dtype or req.dtype
     kw = dict(reconstruct=req.reconstruct, rsolver=req.rsolver,
               tile=tuple(tile) if tile is not None else SERVING_TILES[dtype],
               dtype=getattr(t, dtype), clock=clock)
+    U0 = _device_state(req.problem, n)
     if req.problem == "kh":
-        return Solve(kelvin_helmholtz_tanh(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
+        return Solve(U0, 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
     if req.problem == "smooth":
-        return Solve(smooth_waves(n, n), 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
+        return Solve(U0, 1 / n, 1 / n, 1.0, 1e-10, "rk3", 0.4, req.tlim, 10**7, **kw)
     x, _ = cell_centers(n, n)
     modes = cartesian_modes(3, 5, (-5, 5), (-5, 5))
     updates = int(np.ceil(req.tlim / 0.0075)) + 1
     table = modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, req.seed, 0.75, 0.0075, updates)
     basis = forcing_basis(modes, x, x, (1.0, 1.0))
-    return Solve(uniform_rest(n, n), 1 / n, 1 / n, 1.0, 1.17549e-38, "rk3", 0.4, req.tlim, 10**7,
+    return Solve(U0, 1 / n, 1 / n, 1.0, 1.17549e-38, "rk3", 0.4, req.tlim, 10**7,
                  viscosity=1.5e-6, drag_rate=0.3333335, forcing=(table, basis), dt_update=0.0075,
                  dedt=0.03703705, **kw)
 
@@ -129,26 +152,59 @@ class Server:
         self.builder = builder or build_solve  # (request, tile, clock, dtype) -> Solve
 
     def run(self, requests):
-        """Serve `requests` (arrival-ordered or not); returns a stats dict."""
+        """Serve `requests` (arrival-ordered or not); returns a stats dict.
+
+        The loop is pipelined: each tick enqueues its steps and a snapshot of
+        every clock, then reads the previous tick's snapshot while the GPU
+        runs this one. Solves found finished are retired (box sums for the
+        failure check and, with keep_results, the state copied to pinned host
+        memory, all stream-ordered) and leave the next plan; their memory and
+        clock slot return once those copies have landed. Completion times
+        are the GPU time of the snapshot that first showed the solve done.
+        """
         t = _lib.torch()
         from .batch import Batch, ClockBank
         bank = ClockBank(self.max_live)
-        # One pinned/device pair for every re-plan (a plan is ~2.7 KB per solve).
+        # One pinned/device pair for every re-plan (a plan is ~3 KB per solve).
         plan_cap = 4096 + self.max_live * 4096
         plan_bufs = (t.empty(plan_cap, dtype=t.uint8).pin_memory(),
                      t.empty(plan_cap, dtype=t.uint8, device=_lib.device()))
+        sums_dev = t.empty((self.max_live, 4), dtype=t.float64, device=_lib.device())
+        sums_host = t.empty((self.max_live, 4), dtype=t.float64).pin_memory()
         free_slots = list(range(self.max_live - 1, -1, -1))
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         live = []          # (req, solve, slot)
+        retiring = []      # (req, solve, slot, event, result_host, clock)
         in_use = 0.0
         batch = None
         changed = True
         ticks = 0
         peak_live = 0
         peak_bytes = 0.0
+        previous = None    # (event, host clocks, live list) of the last tick
         t.cuda.synchronize()
+        start = t.cuda.Event(enable_timing=True)
+        start.record()
         t0 = time.perf_counter()
-        while pending or live:
+
+        def finish(entry, wait):
+            req, solve, slot, event, result_host, c = entry
+            if not (wait or event.query()):
+                return False
+            event.synchronize()
+            sums = sums_host[slot, :solve.desc.nvar].numpy()
+            # A non-finite state drives dt to NaN and stops the solve early
+            # (run.py:178-180 raises there); a tracer-only NaN leaves dt
+            # finite, so the box sums are checked as well.
+            if not (c.time == c.tlim or c.cycle >= c.nlim) or not np.isfinite(c.time) \
+                    or not np.all(np.isfinite(sums)):
+                req.error = f"stopped at t={c.time} after {c.cycle} steps (non-finite state)"
+            elif result_host is not None:
+                req.result = result_host.numpy()
+            free_slots.append(slot)
+            return True
+
+        while pending or live or retiring or previous:
             now = time.perf_counter() - t0
             while (pending and pending[0].arrival <= now and free_slots
                    and in_use + footprint_bytes(pending[0], self.dtype) <= self.budget):
@@ -160,44 +216,62 @@ class Server:
                 in_use += footprint_bytes(req, self.dtype)
                 peak_bytes = max(peak_bytes, in_use)
                 changed = True
-            if not live:
-                if pending:
-                    wait = pending[0].arrival - (time.perf_counter() - t0)
-                    if wait > 0:
-                        time.sleep(min(wait, 0.01))
-                    elif in_use + footprint_bytes(pending[0], self.dtype) > self.budget:
-                        raise RuntimeError(f"request {pending[0].rid} does not fit in the HBM budget")
-                continue
-            if changed:
-                batch = Batch([s for _, s, _ in live], blocks_per_sm=self.blocks_per_sm, plan_buffers=plan_bufs)
-                changed = False
-            for _ in range(self.steps_per_tick):
-                batch.enqueue_step()
-            ticks += 1
-            peak_live = max(peak_live, len(live))
-            clocks = bank.read()  # one device-to-host copy of every clock (synchronises)
-            stamp = time.perf_counter() - t0
-            still = []
-            for req, solve, slot in live:
-                c = clocks[slot]
-                if c.done:
-                    req.finished = stamp
-                    req.cycles = c.cycle
-                    # A non-finite state drives dt to NaN and stops the solve
-                    # early (run.py:178-180 raises there); a tracer-only NaN
-                    # leaves dt finite, so the box sums are checked as well.
-                    sums = solve.box_sums()
-                    if not (c.time == c.tlim or c.cycle >= c.nlim) or not np.isfinite(c.time) \
-                            or not np.all(np.isfinite(sums)):
-                        req.error = f"stopped at t={c.time} after {c.cycle} steps (non-finite state)"
-                    elif self.keep_results:
-                        req.result = solve.S.cpu().numpy()
-                    free_slots.append(slot)
-                    in_use -= footprint_bytes(req, self.dtype)
-                    changed = True
+            current = None
+            if live:
+                if changed:
+                    batch = Batch([s for _, s, _ in live], blocks_per_sm=self.blocks_per_sm,
+                                  plan_buffers=plan_bufs)
+                    changed = False
+                for _ in range(self.steps_per_tick):
+                    batch.enqueue_step()
+                ticks += 1
+                peak_live = max(peak_live, len(live))
+                event, host = bank.snapshot()
+                current = (event, host, list(live))
+            # Retirements whose copies have landed free their memory and slot.
+            keep = []
+            for entry in retiring:
+                if finish(entry, wait=not live and previous is None):
+                    in_use -= footprint_bytes(entry[0], self.dtype)
                 else:
-                    still.append((req, solve, slot))
-            live = still
+                    keep.append(entry)
+            retiring = keep
+            if previous is not None:
+                event, host, members = previous
+                event.synchronize()  # the GPU keeps running the tick just enqueued
+                stamp = start.elapsed_time(event) * 1e-3
+                clocks = bank.parse(host)
+                # Members already retired from an earlier snapshot are skipped.
+                still = {id(solve) for _, solve, _ in live}
+                done = {slot for _, solve, slot in members if id(solve) in still and clocks[slot].done}
+                if done:
+                    for req, solve, slot in members:
+                        if slot not in done or id(solve) not in still:
+                            continue
+                        req.finished = stamp
+                        req.cycles = clocks[slot].cycle
+                        nv = solve.desc.nvar
+                        _lib.call("jx_box_sums", ctypes.byref(solve.desc), _lib.ptr(solve.S),
+                                  _lib.ptr(sums_dev[slot]), _lib.ptr(solve.ws), solve.nbytes,
+                                  _lib.stream_handle())
+                        sums_host[slot, :nv].copy_(sums_dev[slot, :nv], non_blocking=True)
+                        result_host = None
+                        if self.keep_results:
+                            result_host = t.empty(solve.S.shape, dtype=solve.S.dtype).pin_memory()
+                            result_host.copy_(solve.S, non_blocking=True)
+                        copied = t.cuda.Event()
+                        copied.record()
+                        retiring.append((req, solve, slot, copied, result_host, clocks[slot]))
+                    live = [e for e in live if e[2] not in done]
+                    changed = True
+            previous = current
+            if not live and not retiring and pending and previous is None:
+                wait = pending[0].arrival - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.01))
+                elif in_use + footprint_bytes(pending[0], self.dtype) > self.budget:
+                    raise RuntimeError(f"request {pending[0].rid} does not fit in the HBM budget")
+        t.cuda.synchronize()
         elapsed = time.perf_counter() - t0
         ok = [r for r in requests if r.error is None]
         tts = np.array([r.finished - r.arrival for r in ok]) if ok else np.array([np.nan])

@@ -25,12 +25,13 @@ class Solve:
                  predict_stress=None, sgs_weights=None, tile=(0, 0), dtype=None, clock=None):
         t = _lib.torch()
         RK_STAGES[integrator]
-        self.U = _lib.to_device(U, dtype)
-        self.desc = make_desc(self.U.shape, self.U.dtype, dx, dy, cs, dfloor, integrator,
+        U_dev = _lib.to_device(U, dtype)
+        self.desc = make_desc(U_dev.shape, U_dev.dtype, dx, dy, cs, dfloor, integrator,
                               viscosity=viscosity, smagorinsky_cs=smagorinsky_cs,
                               drag_rate=drag_rate, reconstruct=reconstruct, rsolver=rsolver,
                               tile=tile)
-        self.S = self.U.clone()
+        # The solve owns its state: copy a caller's device array, adopt a fresh one.
+        self.S = U_dev.clone() if U_dev is U else U_dev
         self.A = t.empty_like(self.S)
         self.B = t.empty_like(self.S)
         self.ws, self.nbytes = _lib.workspace(self.desc)
@@ -56,7 +57,7 @@ class Solve:
                 raise ValueError("clock storage must be 128 uint8 elements")
             clock.copy_(fresh)
             self.clock = clock
-        self._idle_clock = _lib.new_clock(done=1)
+        self._idle_clock = None  # made on first capture
         self.graph = None
         self.graph_steps = 0
         _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.ws),
@@ -94,6 +95,8 @@ class Solve:
     def capture(self, steps):
         """Capture `steps` cycles into a CUDA graph (after a launch on an idle clock)."""
         t = _lib.torch()
+        if self._idle_clock is None:
+            self._idle_clock = _lib.new_clock(done=1)
         self.enqueue_step(self._idle_clock)  # sets per-kernel attributes; changes nothing
         t.cuda.synchronize()
         graph = t.cuda.CUDAGraph()

@@ -102,3 +102,19 @@ def test_batch_rejects_other_tiles_and_wide_states():
                  dtype=torch.float32)
     with pytest.raises(ValueError, match="3 or 4 variables"):
         Batch([wide])
+
+
+def test_batched_forcing_matches_solo_bitwise():
+    """Forced solves of both precisions share one render and one kick sequence per precision."""
+    from jathenax_gb300.batch import Batch
+    specs = [("turb", 32, "float32", "ppm4", "roe", "rk3", 0.03), ("turb", 70, "float32", "wenoz", "hlle", "rk2", 0.02),
+             ("turb", 48, "float64", "ppm4", "roe", "rk3", 0.02), ("turb", 40, "float64", "plm", "llf", "rk4", 0.02),
+             ("kh", 40, "float32", "ppm4", "roe", "rk3", 0.02)]
+    seeds = [3, 5, 7, 11, 13]
+    solves = [make_solve(*spec, tile_y=16, seed=seed) for spec, seed in zip(specs, seeds)]
+    Batch(solves).run(steps_per_sync=4)
+    for spec, seed, s in zip(specs, seeds, solves):
+        alone = make_solve(*spec, tile_y=16, seed=seed)
+        alone.run(steps_per_sync=4)
+        assert s.state().cycle == alone.state().cycle > 2, spec
+        np.testing.assert_array_equal(s.S.cpu().numpy(), alone.S.cpu().numpy(), err_msg=str(spec))
