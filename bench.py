@@ -51,7 +51,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    p.add_argument("--n", type=int, default=4096, help="grid side (default 4096)")
+    p.add_argument("--n", type=int, default=None, help="grid side (default 4096; 1024 with --sweep)")
     p.add_argument("--no-fp32", action="store_true", help="skip the float32 line")
     p.add_argument("--only-fp32", action="store_true", help="time only the float32 state (profiling)")
     p.add_argument("--cpu-sample", type=int, default=512, help="grid side of the CPU sample")
@@ -59,6 +59,9 @@ def parse_args():
     p.add_argument("--no-patterns", action="store_true",
                    help="skip the batched / serving / precision measurements")
     p.add_argument("--serve-requests", type=int, default=100)
+    p.add_argument("--sweep", action="store_true",
+                   help="instead of the benchmark line: one JSON line per reconstruction x Riemann "
+                        "solver x integrator x precision on the --n grid (default 1024 here)")
     return p.parse_args()
 
 
@@ -247,22 +250,44 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
                 dt=state.dt)
 
 
-def cpu_baseline_sample(n, steps):
-    """The float64 oracle (NumPy, one thread) on an n x n sample of the workload."""
+def _oracle_cycles(n, steps, start_at=None):
+    """`steps` float64 oracle RK3 cycles (dt + 3 stages) on an n x n tanh KH state;
+    returns the seconds they took (after waiting for `start_at`, a wall-clock time)."""
     from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
     from oracle import hydro_oracle as H
     U = kelvin_helmholtz_tanh(n, n)
     prev = np.inf
+    if start_at is not None:
+        time.sleep(max(0.0, start_at - time.time()))
     t0 = time.perf_counter()
     for _ in range(steps):
         _, W = H.primitives(U, 1e-10)
         dt = float(H.timestep(W, 1 / n, 1 / n, 1.0, 0.4, prev, 0.0, 1e30))
         U = H.step(U, dt, 1 / n, 1 / n, 1.0, 1e-10, "rk3")
         prev = dt
-    elapsed = time.perf_counter() - t0
-    return dict(value=n * n * steps / elapsed, unit=METRIC, cores=1, kind="port",
-                sample=f"float64 NumPy oracle, kelvin_helmholtz_tanh {n}x{n}, {steps} full RK3 "
-                       f"cycles (dt + 3 stages), single thread", seconds=round(elapsed, 2))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline_sample(n, steps, procs=None):
+    """The float64 oracle (NumPy) on n x n samples of the workload, one independent
+    sample per host core in `spawn`ed processes that start together; the rate is
+    the total cell-updates over the slowest process's time."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    procs = procs or os.cpu_count() or 1
+    if procs == 1:
+        elapsed = [_oracle_cycles(n, steps)]
+    else:
+        # spawn: this process may already hold a CUDA context. A worker that
+        # dies raises BrokenProcessPool here instead of hanging the pool.
+        with ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as pool:
+            start_at = time.time() + 10.0  # every worker has imported NumPy by then
+            elapsed = list(pool.map(_oracle_cycles, [n] * procs, [steps] * procs, [start_at] * procs))
+    slowest = max(elapsed)
+    return dict(value=procs * n * n * steps / slowest, unit=METRIC, cores=procs, kind="port",
+                sample=f"float64 NumPy oracle, kelvin_helmholtz_tanh {n}x{n}, {steps} full RK3 cycles "
+                       f"(dt + 3 stages) in each of {procs} processes (one per host core)",
+                seconds=round(slowest, 2))
 
 
 def bench_ours(args, world, rank, local):
@@ -376,7 +401,7 @@ def bench_batched(torch, tlim=0.02):
     from jathenax_gb300.diagnostics import relative_l1
     from jathenax_gb300.serve import build_solve
     reqs = [make_request(k, n, s, tlim, "float32", i) for i, (k, n, s) in enumerate(ensemble_specs())]
-    tuned = autotune.tune("float32", "ppm4", "roe", 4, 1024)
+    tuned = autotune.tune_batch(lambda tile: [build_solve(r, tile) for r in reqs])
     bank = ClockBank(len(reqs))
     solves = [build_solve(r, tuned["tile"], clock=bank.slot(i)) for i, r in enumerate(reqs)]
     batch = Batch(solves, blocks_per_sm=tuned["blocks_per_sm"], clocks=bank)
@@ -403,34 +428,57 @@ def bench_batched(torch, tlim=0.02):
             "speedup": round(serial_s / batched_s, 2),
             "max_l1_density_err_fp32_vs_fp64": max(l1),
             "tile": tuned["tile"], "blocks_per_sm": tuned["blocks_per_sm"],
+            "autotune_ms_per_step": {f"{t['tile'][0]}x{t['tile'][1]}": round(t["ms_per_step"], 3)
+                                     for t in tuned["trials"]},
             "batched_s": round(batched_s, 3), "serial_s": round(serial_s, 3)}
 
 
 def bench_serving(torch, n):
     """Scaled serving stream: Poisson arrivals, side log-uniform 64..512, tlim U[0.02, 0.2],
-    80% float32; continuous batching vs serial plain float64."""
+    80% float32; continuous batching vs serial plain float64, at a light and a heavy rate
+    (the same requests; only the arrival times differ)."""
     from jathenax_gb300.diagnostics import relative_l1
     from jathenax_gb300.serve import Server, make_stream, run_serial
-    def stream():
-        return make_stream(n, rate=200.0, seed=2026, side_range=(64, 512), tlim_range=(0.02, 0.2))
 
-    ref = stream()
+    def stream(rate):
+        return make_stream(n, rate=rate, seed=2026, side_range=(64, 512), tlim_range=(0.02, 0.2))
+
+    ref = stream(200.0)
     serial = run_serial(ref, dtype="float64", keep_results=True)
-    out = {"requests": n, "stream": "Poisson 200/s, side log-uniform 64..512, tlim U[0.02,0.2], problems "
+    out = {"requests": n, "stream": "Poisson arrivals, side log-uniform 64..512, tlim U[0.02,0.2], problems "
            "smooth/kh/turbulence, random recon/rsolver, 150 GB budget",
            "serial_fp64_solves_per_s": round(serial["solves_per_s"], 3)}
-    for label, dtype in (("mixed_80pct_fp32", None), ("all_fp32", "float32")):
-        reqs = stream()
-        stats = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype).run(reqs)
-        errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs)
-                if (dtype or q.dtype) == "float32"]
-        out[label] = {"solves_per_s": round(stats["solves_per_s"], 3),
-                      "speedup_vs_serial_fp64": round(stats["solves_per_s"] / serial["solves_per_s"], 2),
-                      "tts_p50_s": round(stats["tts_p50_s"], 4), "tts_p99_s": round(stats["tts_p99_s"], 4),
-                      "peak_live": stats["peak_live"],
-                      "fp32_l1_density_err_vs_fp64_max": max(errs) if errs else None,
-                      "fp32_l1_density_err_vs_fp64_median": float(np.median(errs)) if errs else None}
+    for rate in (200.0, 1000.0):
+        for label, dtype in (("mixed_80pct_fp32", None), ("all_fp32", "float32")):
+            reqs = stream(rate)
+            stats = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype).run(reqs)
+            errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs)
+                    if (dtype or q.dtype) == "float32"]
+            out[f"{label}_rate{int(rate)}"] = {
+                "solves_per_s": round(stats["solves_per_s"], 3),
+                "speedup_vs_serial_fp64": round(stats["solves_per_s"] / serial["solves_per_s"], 2),
+                "tts_p50_s": round(stats["tts_p50_s"], 4), "tts_p99_s": round(stats["tts_p99_s"], 4),
+                "peak_live": stats["peak_live"],
+                "fp32_l1_density_err_vs_fp64_max": max(errs) if errs else None,
+                "fp32_l1_density_err_vs_fp64_median": float(np.median(errs)) if errs else None}
     return out
+
+
+def driven_turbulence(side, tlim, dtype, smagorinsky_cs=0.0, seed=1618):
+    """The reference's driven-turbulence run (input.py:43-47 forcing, run.py:133-158):
+    rest state, 56 parabolic modes (3 <= |k| <= 5), seed 1618, nu 1.5e-6, drag 0.3333335."""
+    import torch
+    from jathenax_gb300.forcing import cartesian_modes, forcing_basis, modal_coefficients
+    from jathenax_gb300.initial_conditions import cell_centers, uniform_rest
+    from jathenax_gb300.solver import Solve
+    x, _ = cell_centers(side, side)
+    modes = cartesian_modes(3, 5, (-5, 5), (-5, 5))
+    updates = int(np.ceil(tlim / 0.0075)) + 1
+    table = modal_coefficients(modes, (1.0, 1.0), 3, 5, 4.0, 1.0, seed, 0.75, 0.0075, updates)
+    basis = forcing_basis(modes, x, x, (1.0, 1.0))
+    return Solve(uniform_rest(side, side), 1 / side, 1 / side, 1.0, 1.17549e-38, "rk3", 0.4, tlim, 10**8,
+                 viscosity=1.5e-6, smagorinsky_cs=smagorinsky_cs, drag_rate=0.3333335,
+                 forcing=(table, basis), dt_update=0.0075, dedt=0.03703705, dtype=getattr(torch, dtype))
 
 
 def bench_precision(torch):
@@ -438,14 +486,27 @@ def bench_precision(torch):
     from jathenax_gb300.diagnostics import precision_report
     from jathenax_gb300.serve import build_solve
     out = {}
-    for kind, side, tlim in (("kh", 512, 0.05), ("turbulence", 256, 0.1)):
-        res = {}
+    runs = [("kh_512_t0.05", lambda dt: build_solve(make_request("kh", 512, 1618, 0.05, dt), dtype=dt)),
+            ("turbulence_256_t0.1",
+             lambda dt: build_solve(make_request("turbulence", 256, 1618, 0.1, dt), dtype=dt)),
+            ("turbulence_1024_t1", lambda dt: driven_turbulence(1024, 1.0, dt)),
+            ("turbulence_smagorinsky0.17_1024_t1", lambda dt: driven_turbulence(1024, 1.0, dt, 0.17))]
+    for name, make in runs:
+        res, cycles, seconds = {}, {}, {}
         for dtype in ("float32", "float64"):
-            s = build_solve(make_request(kind, side, 1618, tlim, dtype), dtype=dtype)
+            s = make(dtype)
             U0 = s.S.cpu().numpy().astype(np.float64)
-            s.run(steps_per_sync=32)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run(steps_per_sync=64)
+            torch.cuda.synchronize()
+            seconds[dtype] = round(time.perf_counter() - t0, 3)
             res[dtype] = s.S.cpu().numpy()
-        out[f"{kind}_{side}_t{tlim}"] = precision_report(res["float32"], res["float64"], U0, 1 / side, 1 / side)
+            cycles[dtype] = s.state().cycle
+            del s
+        side = res["float64"].shape[0]
+        out[name] = precision_report(res["float32"], res["float64"], U0, 1 / side, 1 / side)
+        out[name].update(cycles=cycles, seconds=seconds)
     return out
 
 
@@ -467,8 +528,47 @@ def bench_reference(args, world, rank):
     }
 
 
+def bench_sweep(args):
+    """cell-updates/s of every method combination (graph replays of whole cycles)."""
+    import torch
+    from jathenax_gb300 import _lib
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from jathenax_gb300.solver import Solve
+    n = args.n or 1024
+    U0 = torch.as_tensor(kelvin_helmholtz_tanh(n, n), device="cuda")
+    for dtype in (torch.float64, torch.float32):
+        for recon in ("dc", "plm", "ppm4", "ppmx", "wenoz"):
+            for rsolver in ("llf", "hlle", "roe"):
+                for integrator in ("rk2", "rk3", "rk4"):
+                    s = Solve(U0, 1.0 / n, 1.0 / n, 1.0, 1e-10, integrator, 0.4, 1e30, 2**31 - 1,
+                              reconstruct=recon, rsolver=rsolver, dtype=dtype)
+                    s.capture(1)
+                    for _ in range(args.warmup):
+                        s.graph.replay()
+                    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    torch.cuda.synchronize()
+                    start.record()
+                    for _ in range(args.steps):
+                        s.graph.replay()
+                    end.record()
+                    torch.cuda.synchronize()
+                    ms = start.elapsed_time(end) / args.steps
+                    tx, ty, smem = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+                    _lib.call("jx_tile_info", ctypes.byref(s.desc), ctypes.byref(tx), ctypes.byref(ty),
+                              ctypes.byref(smem))
+                    print(json.dumps({"sweep": f"{recon}/{rsolver}/{integrator}", "dtype": str(dtype)[6:],
+                                      "n": n, "ms_per_step": round(ms, 4),
+                                      "value": round(n * n / (ms * 1e-3), 1), "unit": METRIC,
+                                      "tile": [tx.value, ty.value]}), flush=True)
+                    del s
+
+
 def main():
     args = parse_args()
+    if args.sweep:
+        bench_sweep(args)
+        return
+    args.n = args.n or 4096
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         line = bench_reference(args, world, rank)

@@ -1,7 +1,7 @@
 """Autotuner for the batched stage kernels.
 
 Searches the stage tile (the shared-memory kernel's 32 x 8, 16 or 32 tiles
-of 256 threads, and the register-marching kernel's 58 x 16 / 32 / 64 tiles
+of 256 threads, and the register-marching kernel's 58 x 8 / 16 / 32 tiles
 of 128 threads) and the number of persistent blocks per SM (occupancy limit
 or 1..4) for one (precision, reconstruction, Riemann solver, variable count)
 kernel class on a probe grid, timing a few evolve cycles of each candidate
@@ -18,7 +18,7 @@ from pathlib import Path
 
 from . import _lib
 
-TILES = ((32, 8), (32, 16), (32, 32), (58, 16), (58, 32), (58, 64))
+TILES = ((32, 8), (32, 16), (32, 32), (58, 8), (58, 16), (58, 32))
 BLOCKS_PER_SM = (0, 1, 2, 3, 4)
 _memory = {}
 
@@ -98,3 +98,38 @@ def tune(dtype="float32", reconstruct="ppm4", rsolver="roe", nvar=4, side=1024, 
     _memory[key] = result
     _store(key, result)
     return result
+
+
+def tune_batch(make_solves, tiles=TILES, blocks_per_sm=(0,), steps=3, warmup=2):
+    """Pick the tile (and persistent blocks per SM) for one particular set of
+    solves, timing the batched cycle itself rather than a probe grid.
+
+    ``make_solves(tile)`` returns fresh Solve objects built with that tile;
+    each candidate runs ``warmup`` untimed and ``steps`` timed batched cycles.
+    Returns {"tile", "blocks_per_sm", "ms_per_step", "trials"} (not cached:
+    the answer belongs to the solve set).
+    """
+    t = _lib.torch()
+    from .batch import Batch
+    trials = []
+    for tile in tiles:
+        for bps in blocks_per_sm:
+            try:
+                solves = make_solves(tuple(tile))
+            except (ValueError, RuntimeError):  # tile does not fit in shared memory
+                continue
+            batch = Batch(solves, blocks_per_sm=bps)
+            for _ in range(warmup):
+                batch.enqueue_step()
+            start, end = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            start.record()
+            for _ in range(steps):
+                batch.enqueue_step()
+            end.record()
+            end.synchronize()
+            trials.append({"tile": list(tile), "blocks_per_sm": bps, "ms_per_step": start.elapsed_time(end) / steps})
+            del batch, solves
+    if not trials:
+        raise RuntimeError("no autotuning candidate could run")
+    best = min(trials, key=lambda r: r["ms_per_step"])
+    return dict(best, trials=trials)

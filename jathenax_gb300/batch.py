@@ -62,7 +62,7 @@ class Batch:
     ``tile=(32, h)`` / ``tile=(58, h)`` at construction).
     """
 
-    def __init__(self, solves, blocks_per_sm=0, clocks=None, plan_buffers=None):
+    def __init__(self, solves, blocks_per_sm=0, clocks=None):
         t = _lib.torch()
         self.solves = list(solves)
         if not self.solves:
@@ -74,15 +74,14 @@ class Batch:
         size = ctypes.c_size_t()
         _lib.call("jx_batch_plan_bytes", arr, n, ctypes.byref(size))
         nbytes = int(size.value)
-        if plan_buffers is not None and plan_buffers[0].numel() >= nbytes:
-            # Reused (host pinned, device) pair, e.g. a server re-planning every tick.
-            self.plan_host, self.plan_dev = plan_buffers[0][:nbytes], plan_buffers[1][:nbytes]
-        else:
-            self.plan_host = t.empty(nbytes, dtype=t.uint8).pin_memory()
-            self.plan_dev = t.empty(nbytes, dtype=t.uint8, device=_lib.device())
+        # Each plan gets its own buffers from torch's caching allocators: the
+        # pinned host block is not handed out again until the asynchronous
+        # copy below has run, and the device block is reused only in stream
+        # order. (Rewriting one pinned buffer for every re-plan would race
+        # with a copy the GPU has not yet reached.)
+        self.plan_host = t.empty(nbytes, dtype=t.uint8, pin_memory=True)
+        self.plan_dev = t.empty(nbytes, dtype=t.uint8, device=_lib.device())
         _lib.call("jx_batch_plan", arr, n, ctypes.c_void_p(self.plan_host.data_ptr()), nbytes)
-        # Stream-ordered copy: earlier steps that read an older plan in the same
-        # buffer are enqueued before it.
         self.plan_dev.copy_(self.plan_host, non_blocking=True)
         self.groups = _lib.load().jx_batch_groups(ctypes.c_void_p(self.plan_host.data_ptr()))
         self.graph = None

@@ -120,7 +120,7 @@ __device__ __forceinline__ void velocity_at(const R* X, int nx, int nv, R dfloor
   } else {
     R r = x[0];
     r = r < dfloor ? dfloor : r;
-    const R inv = R(1) / r;
+    const R inv = Num<R>::rcp(r);
     rho = r;
     vx = inv * x[1];
     vy = inv * x[2];
@@ -466,7 +466,7 @@ __global__ void recover_kernel(const R* U, R* Uo, R* W, int64_t ncell, int nv, R
   const R* u = U + k * nv;
   R rho = u[0];
   rho = rho < dfloor ? dfloor : rho;
-  const R inv = R(1) / rho;
+  const R inv = Num<R>::rcp(rho);
   if (Uo) {
     Uo[k * nv] = rho;
     for (int c = 1; c < nv; ++c) Uo[k * nv + c] = u[c];

@@ -24,11 +24,14 @@ def evolve_isothermal(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *,
                       viscosity=0.0, smagorinsky_cs=0.0, drag_rate=0.0,
                       forcing=None, dt_update=1.0, tdriv_start=0.0, dedt=0.0,
                       reconstruct="ppm4", rsolver="roe", predict_stress=None, sgs_weights=None,
-                      steps_per_sync=32):
+                      steps_per_sync=32, checkpoint=None, checkpoint_every=0, resume=None):
     """Advance the device-resident periodic grid to tlim or nlim cycles (run.py:20-69).
 
     ``forcing`` is ``(coefficients, basis)`` from modal_coefficients and
     forcing_basis. Time and dt are accumulated in float64 on the device.
+    Added (no reference counterpart): ``resume`` continues from a checkpoint
+    npz of the same problem instead of from U; ``checkpoint`` writes one
+    every ``checkpoint_every`` cycles and at the end (Solve.checkpoint).
     """
     check_evolve_args(viscosity, smagorinsky_cs, drag_rate, dedt, forcing, dt_update, tdriv_start)
     solve = Solve(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, viscosity=viscosity,
@@ -36,7 +39,9 @@ def evolve_isothermal(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *,
                   dt_update=dt_update, tdriv_start=tdriv_start, dedt=dedt,
                   reconstruct=reconstruct, rsolver=rsolver, predict_stress=predict_stress,
                   sgs_weights=sgs_weights)
-    solve.run(steps_per_sync=steps_per_sync)
+    if resume is not None:
+        solve.resume(resume)
+    solve.run(steps_per_sync=steps_per_sync, checkpoint=checkpoint, checkpoint_every=checkpoint_every)
     S, time, dt, cycle = solve.result()
     if _lib.is_device_array(U):
         t = _lib.torch()
@@ -62,6 +67,10 @@ def main(argv=None):
     parser.add_argument("--output", type=Path, help="Output .npz file")
     parser.add_argument("--precision", choices=("float64", "float32"), default="float64",
                         help="State precision on the GPU (default: float64)")
+    parser.add_argument("--checkpoint", type=Path,
+                        help="Write a resumable checkpoint npz here (every --checkpoint-every cycles and at the end)")
+    parser.add_argument("--checkpoint-every", type=int, default=0, help="Cycles between checkpoints")
+    parser.add_argument("--resume", type=Path, help="Continue from a checkpoint of the same problem")
     args = parser.parse_args(argv)
     try:
         settings = read_input(args.input, args.problem)
@@ -142,7 +151,8 @@ def main(argv=None):
         viscosity=viscosity, smagorinsky_cs=smagorinsky_cs, drag_rate=drag_rate,
         forcing=forcing, dt_update=dt_update, tdriv_start=tdriv_start, dedt=dedt,
         reconstruct=reconstruct, rsolver=rsolver,
-        predict_stress=predict_stress, sgs_weights=sgs_weights)
+        predict_stress=predict_stress, sgs_weights=sgs_weights,
+        checkpoint=args.checkpoint, checkpoint_every=args.checkpoint_every, resume=args.resume)
     reached_tlim = time == np.float64(tlim)
     if not np.isfinite(U).all() or not np.isfinite(time) or (not reached_tlim and cycle != nlim):
         raise RuntimeError(f"Periodic run ended at t={time} after {cycle} steps")

@@ -9,6 +9,7 @@ replay a CUDA graph of ``steps_per_sync`` captured cycles.
 """
 
 import ctypes
+import json
 
 import numpy as np
 
@@ -129,27 +130,93 @@ class Solve:
         js.workspace_bytes = self.nbytes
         return js
 
-    def run(self, steps_per_sync=32, use_graph=True):
-        """Advance until tlim or nlim; returns the final clock."""
+    def run(self, steps_per_sync=32, use_graph=True, checkpoint=None, checkpoint_every=0):
+        """Advance until tlim or nlim; returns the final clock.
+
+        With ``checkpoint`` (a path) the run is written there (see
+        :meth:`checkpoint`) whenever ``checkpoint_every`` more cycles have
+        completed (checked every ``steps_per_sync`` cycles) and at the end.
+        """
+        last = self.state().cycle
         if self.predict_stress is not None:
             while self._hooked_step():
-                pass
-            return self.state()
-        if use_graph and self.graph is None:
-            self.capture(steps_per_sync)
-        while True:
-            if use_graph:
-                self.graph.replay()
-            else:
-                for _ in range(steps_per_sync):
-                    self.enqueue_step()
-            clock = self.state()
-            if clock.done:
-                return clock
+                last = self._maybe_checkpoint(checkpoint, checkpoint_every, last)
+        else:
+            if use_graph and self.graph is None:
+                self.capture(steps_per_sync)
+            while True:
+                if use_graph:
+                    self.graph.replay()
+                else:
+                    for _ in range(steps_per_sync):
+                        self.enqueue_step()
+                if self.state().done:
+                    break
+                last = self._maybe_checkpoint(checkpoint, checkpoint_every, last)
+        if checkpoint is not None:
+            self.checkpoint(checkpoint)
+        return self.state()
+
+    def _maybe_checkpoint(self, path, every, last):
+        if path is None or every <= 0:
+            return last
+        cycle = self.state().cycle
+        if cycle - last >= every:
+            self.checkpoint(path)
+            return cycle
+        return last
 
     def result(self):
         c = self.state()
         return self.S, c.time, c.prev_dt, c.cycle
+
+    # -- checkpoint / resume ----------------------------------------------------
+    def _desc_fields(self):
+        return {name: getattr(self.desc, name) for name, _ in self.desc._fields_}
+
+    def checkpoint(self, path):
+        """Write the resident run to an npz file for an exact resume.
+
+        Keys: ``conserved``, ``time``, ``dt`` and ``cycle`` as in the
+        reference's output (run.py:184-185), plus what an exact resume needs:
+        ``clock`` (the 128-byte device clock), ``workspace`` (the CFL partials
+        the next dt is chosen from, the forcing sums), ``raw_force`` (the
+        cached forcing field of a forced run) and ``desc`` (the problem
+        description, checked on resume).
+        """
+        c = self.state()
+        arrays = dict(conserved=self.S.cpu().numpy(), time=np.float64(c.time), dt=np.float64(c.prev_dt),
+                      cycle=np.int32(c.cycle), clock=self.clock.cpu().numpy(),
+                      workspace=self.ws.cpu().numpy(), desc=np.array(json.dumps(self._desc_fields())))
+        if self.forcing is not None:
+            arrays["raw_force"] = self.forcing.raw.cpu().numpy()
+        np.savez(path, **arrays)
+
+    def resume(self, path):
+        """Continue from a checkpoint written by a Solve built with the same
+        arguments (the end time, cycle limit and forcing-table length may be
+        larger); the continued run is bitwise the uninterrupted one."""
+        t = _lib.torch()
+        with np.load(path, allow_pickle=False) as data:
+            if json.loads(str(data["desc"])) != self._desc_fields():
+                raise ValueError("checkpoint was written for a different problem description")
+            U = data["conserved"]
+            if tuple(U.shape) != tuple(self.S.shape) or U.dtype != np.dtype(str(self.S.dtype)[6:]):
+                raise ValueError("checkpoint state does not match this solve's shape and precision")
+            if ("raw_force" in data) != (self.forcing is not None):
+                raise ValueError("checkpoint and solve disagree about forcing")
+            if data["workspace"].size != self.nbytes or data["clock"].size != 128:
+                raise ValueError("checkpoint workspace or clock has the wrong size")
+            # The saved clock carries time, cycle, dt history and the forcing
+            # schedule; the limits are this solve's, and begin-step re-tests them.
+            mine = self.state()
+            c = _lib.Clock.from_buffer_copy(data["clock"].tobytes())
+            c.tlim, c.nlim, c.n_updates, c.done = mine.tlim, mine.nlim, mine.n_updates, 0
+            self.S.copy_(t.from_numpy(U))
+            self.clock.copy_(t.from_numpy(np.frombuffer(bytes(c), dtype=np.uint8).copy()))
+            self.ws.copy_(t.from_numpy(data["workspace"]))
+            if self.forcing is not None:
+                self.forcing.raw.copy_(t.from_numpy(data["raw_force"]))
 
     def advance_host(self, U_host, out_host, steps=1):
         """Load U from host memory, advance `steps` cycles, write the state back.

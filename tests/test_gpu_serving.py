@@ -54,3 +54,19 @@ def test_a_failing_request_is_retired_and_the_others_complete():
     assert stats["failed"] == 1 and stats["completed"] == 5
     assert reqs[2].error is not None and "non-finite" in reqs[2].error
     assert all(r.error is None for r in reqs if r.rid != victim)
+
+
+def test_replanning_every_tick_keeps_results_exact():
+    """Many short requests and one step per tick: the batch is re-planned at
+    almost every tick while earlier ticks are still queued on the GPU."""
+    from jathenax_gb300.serve import Server, build_solve, make_stream
+    reqs = make_stream(24, 2000.0, seed=8, side_range=(16, 64), tlim_range=(0.05, 0.3), fp32_fraction=0.7)
+    for _ in range(2):
+        for r in reqs:
+            r.admitted = r.finished = r.result = None
+        stats = Server(budget_bytes=1e9, steps_per_tick=1, keep_results=True).run(reqs)
+        assert stats["completed"] == len(reqs) and stats["ticks"] > len(reqs)
+    for r in reqs:
+        alone = build_solve(r)
+        alone.run(steps_per_sync=4)
+        np.testing.assert_array_equal(r.result, alone.S.cpu().numpy(), err_msg=str(r))
