@@ -95,6 +95,7 @@ PROTOTYPES = {
     "jx_box_sums": [_DP, _P, _P, _P, _SZ, _P],
     "jx_tile_info": [_DP, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
     "jx_probe_fma": [_I32, _I32, _I32, _P, _P],
+    "jx_probe_math": [_I32, _I64, _P, _P, _P, _P, _P, _P],
     "jx_batch_plan_bytes": [ctypes.POINTER(SolveStruct), _I32, ctypes.POINTER(_SZ)],
     "jx_batch_plan": [ctypes.POINTER(SolveStruct), _I32, _P, _SZ],
     "jx_batch_step": [_P, _P, _I32, _P],

@@ -663,6 +663,15 @@ jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sin
   return cuda_check(launch_probe(dtype, blocks, iters, sink, (cudaStream_t)s), "probe kernel");
 }
 
+jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, void* rcp_out, void* div_out,
+                        void* geo_out, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (n < 0 || (n > 0 && (!a || !b || !rcp_out || !div_out || !geo_out)))
+    return fail(JX_ERR_INVALID, "bad probe arguments");
+  return cuda_check(launch_math_probe(dtype, n, a, b, rcp_out, div_out, geo_out, (cudaStream_t)s),
+                    "math probe kernel");
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

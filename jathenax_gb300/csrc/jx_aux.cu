@@ -821,6 +821,28 @@ cudaError_t launch_box_sums(int dtype, const void* U, int64_t ncell, int nv, dou
   return cudaGetLastError();
 }
 
+template <typename R>
+__global__ void math_probe_kernel(int64_t n, const R* a, const R* b, R* rcp_out, R* div_out, R* geo_out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  rcp_out[k] = Num<R>::rcp(b[k]);
+  div_out[k] = Num<R>::div(a[k], b[k]);
+  geo_out[k] = Num<R>::geo_mean(fabs(a[k]), fabs(b[k]));
+}
+
+cudaError_t launch_math_probe(int dtype, int64_t n, const void* a, const void* b, void* rcp_out, void* div_out,
+                              void* geo_out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = (int)((n + 255) / 256);
+  if (dtype == JX_F64)
+    math_probe_kernel<double><<<g, 256, 0, s>>>(n, (const double*)a, (const double*)b, (double*)rcp_out,
+                                                (double*)div_out, (double*)geo_out);
+  else
+    math_probe_kernel<float><<<g, 256, 0, s>>>(n, (const float*)a, (const float*)b, (float*)rcp_out,
+                                               (float*)div_out, (float*)geo_out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_probe(int dtype, int blocks, int iters, double* sink, cudaStream_t s) {
   if (dtype == JX_F64) fma_probe_kernel<double><<<blocks, 256, 0, s>>>(iters, sink);
   else fma_probe_kernel<float><<<blocks, 256, 0, s>>>(iters, sink);

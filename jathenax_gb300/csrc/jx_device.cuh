@@ -16,13 +16,16 @@
 // exception: a product a*b that underflows to +-0 is classified by the signs
 // of a and b); NaN operands are treated as large numbers instead of being
 // skipped by fmin/fmax, which only matters for a state that has already
-// failed. Single precision uses the native instructions, and takes the
-// reciprocals and square roots of the primitive recovery, the Riemann
-// solvers' Roe averages and wave-speed weights and the CFL speeds from the
-// special-function unit's approximations (PTX rcp.approx.f32 and
-// sqrt.approx.f32, at most about one unit in the last place off) instead of
-// the correctly rounded sequences; float64 keeps correctly rounded division
-// and square root.
+// failed. Single precision uses the native instructions.
+//
+// Reciprocals and quotients (primitive recovery, Riemann solvers, PLM/PPMX/
+// WENO-Z weights, CFL speeds) go through Num<R>::rcp/div. In float32 both use
+// the special-function unit's approximations (PTX rcp.approx.f32,
+// sqrt.approx.f32, about one unit in the last place). In float64 the
+// reciprocals of the recovery, the Riemann solvers and the CFL speeds are a
+// Newton-Raphson refinement of the unit's float64 seed (within an ulp; the
+// tolerance against the reference is 1e-12 per stage), and quotients stay
+// correctly rounded.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -79,7 +82,15 @@ template <> struct Num<float> {
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
   }
-  static __device__ __forceinline__ float div(float a, float b) { return a * rcp(b); }
+  // a/b as a (1/b), except where 1/b overflows (b zero or subnormal), b or a
+  // is not finite: there a/b itself.
+  static __device__ __forceinline__ float div(float a, float b) {
+    const unsigned eb = (__float_as_uint(b) >> 23) & 0xff, ea = (__float_as_uint(a) >> 23) & 0xff;
+    if (eb == 0 || eb == 0xff || ea == 0xff) return a / b;
+    return a * rcp(b);
+  }
+  // sqrt(a) sqrt(b) for a, b >= 0
+  static __device__ __forceinline__ float geo_mean(float a, float b) { return root(a) * root(b); }
 };
 
 template <> struct Num<double> {
@@ -125,8 +136,38 @@ template <> struct Num<double> {
     const long long x = bits(a) & kMag, y = bits(b) & kMag;
     return y > x ? __longlong_as_double(y) : __longlong_as_double(x);
   }
-  static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+  // True when x is zero, subnormal, below 2^-999, above 2^977, or not
+  // finite: there the flush-to-zero seed below (or its reciprocal) leaves the
+  // normal range, and the correctly rounded operation is used instead.
+  static __device__ __forceinline__ bool outside_seed_range(double x) {
+    const long long e = (bits(x) >> 52) & 0x7ff;  // biased exponent
+    return e < 24 || e > 2000;
+  }
+  // 1/x by Newton-Raphson refinement of the special-function unit's seed
+  // (PTX rcp.approx.ftz.f64): each step y <- y + y (1 - x y) squares the
+  // relative error (Flynn, "On division by functional iteration", IEEE TC
+  // 1970); two steps take the seed to within about an ulp of 1/x (checked
+  // against correctly rounded division by the tests). Four DFMA instead of
+  // the longer correctly rounded sequence; float64 parity allows the ulp.
+  static __device__ __forceinline__ double rcp(double x) {
+    if (outside_seed_range(x)) return 1.0 / x;
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double r = fma(-x, y, 1.0);
+    y = fma(y, r, y);
+    r = fma(-x, y, 1.0);
+    return fma(y, r, y);
+  }
   static __device__ __forceinline__ double root(double x) { return sqrt(x); }
+  // sqrt(a) sqrt(b) for a, b >= 0 with one square root, sqrt(a b), unless
+  // the product leaves the normal range.
+  static __device__ __forceinline__ double geo_mean(double a, double b) {
+    const double p = a * b;
+    const long long e = (bits(p) >> 52) & 0x7ff;
+    return (e == 0 || e == 0x7ff) ? sqrt(a) * sqrt(b) : sqrt(p);
+  }
+  // a/b correctly rounded. (The reconstruction weights that divide are
+  // kept exact in float64; see the note above.)
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
 };
 
@@ -207,7 +248,7 @@ __device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face
   const R scale = N::pmax(fabs(m1), N::pmax(fabs(c), fabs(p1)));
   const bool use = agree && N::pgt(fabs(d2), R(1e-12) * scale);
   R ratio = R(0);
-  if (use) ratio = lim / d2;
+  if (use) ratio = N::div(lim, d2);
   const R lm = N::abs_ge_twice(dl, dh) ? c - R(2) * dh : lo_face;
   const R hm = N::abs_ge_twice(dh, dl) ? c - R(2) * dl : hi_face;
   lo = ext ? c + dl * ratio : lm;
@@ -221,7 +262,7 @@ __device__ __forceinline__ void plm_cell(R m1, R c, R p1, R& lo, R& hi) {
   const R bw = c - m1;
   const R fw = p1 - c;
   R hs = R(0);
-  if (N::prod_gt0(bw, fw)) hs = (bw * fw) / (bw + fw);
+  if (N::prod_gt0(bw, fw)) hs = N::div(bw * fw, bw + fw);
   hi = c + hs;
   lo = c - hs;
 }
@@ -233,7 +274,7 @@ __device__ __forceinline__ R wenoz_combine(R s0, R s1, R s2, R s3, R s4, R w0, R
   const R f0 = R(2) * s0 - R(7) * s1 + R(11) * s2;
   const R f1 = -s1 + R(5) * s2 + R(2) * s3;
   const R f2 = R(2) * s2 + R(5) * s3 - s4;
-  return (f0 * a0 + f1 * a1 + f2 * a2) / (R(6) * (a0 + a1 + a2));
+  return Num<R>::div(f0 * a0 + f1 * a1 + f2 * a2, R(6) * (a0 + a1 + a2));
 }
 
 template <typename R>
@@ -251,11 +292,11 @@ __device__ __forceinline__ void wenoz_cell(R m2, R m1, R c, R p1, R p2, R& lo, R
   const R tau = fabs(b0 - b2);
   const R d0 = b0 + eps, d1 = b1 + eps, d2 = b2 + eps;
   const R dmin = N::pmin(d0, N::pmin(d1, d2));
-  const R inv_sc = R(1) / N::pmax(tau, dmin);
+  const R inv_sc = N::div(R(1), N::pmax(tau, dmin));
   R base = dmin * inv_sc;
   base = base * base;
   const R con = tau * inv_sc;
-  const R r0 = con * (dmin / d0), r1 = con * (dmin / d1), r2 = con * (dmin / d2);
+  const R r0 = con * N::div(dmin, d0), r1 = con * N::div(dmin, d1), r2 = con * N::div(dmin, d2);
   const R w0 = base + r0 * r0, w1 = base + r1 * r1, w2 = base + r2 * r2;
   hi = wenoz_combine(m2, m1, c, p1, p2, w0, w1, w2);
   lo = wenoz_combine(p2, p1, c, m1, m2, w2, w1, w0);
@@ -322,8 +363,10 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
                                           R& f0, R& f1, R& f2) {
   // fluxes.py:186-201.
   using N = Num<R>;
-  const R sl = N::root(dl), sr = N::root(dr);
-  const R u = (sl * ul + sr * ur) * N::rcp(sl + sr);
+  // Roe average (sl ul + sr ur) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
+  // multiplied through by sl: (dl ul + r ur) / (dl + r), r = sqrt(dl dr).
+  const R r = N::geo_mean(dl, dr);
+  const R u = fma(r, ur, dl * ul) * N::rcp(dl + r);
   const R alo = N::min(u - g.cs, ul - g.cs);
   const R ahi = N::max(u + g.cs, ur + g.cs);
   const R bm = N::lt0(alo) ? alo : R(-1e-20);
@@ -347,10 +390,12 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
   const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
   const R a0 = R(0.5) * (l0 + r0), a1 = R(0.5) * (l1 + r1), a2 = R(0.5) * (l2 + r2);
-  const R sl = N::root(dl), sr = N::root(dr);
-  const R inv = N::rcp(sl + sr);
-  const R u = (sl * ul + sr * ur) * inv;
-  const R t = (sl * tl + sr * tr) * inv;
+  // Roe averages (sl v_l + sr v_r) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
+  // multiplied through by sl: (dl v_l + r v_r) / (dl + r), r = sqrt(dl dr).
+  const R r = N::geo_mean(dl, dr);
+  const R inv = N::rcp(dl + r);
+  const R u = fma(r, ur, ml) * inv;
+  const R t = fma(r, tr, ql) * inv;
   const R lm = u - g.cs, lp = u + g.cs;
   const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
   const R hu = (R(0.5) * u) * g.inv_cs;

@@ -1,13 +1,20 @@
-"""Diagnostics on host copies of states: spectra, errors, conservation drift.
+"""Diagnostics on host copies of states: spectra, fields, errors, drift.
 
 ``shell_spectra`` restates the reference's analysis script
 (jathenax/spectra.py:22-41): density-weighted kinetic energy of sqrt(rho) v
 and the Fourier-curl enstrophy, summed over integer shells
-floor(|k| + 0.5), without plotting. The error helpers are the Precision
-pattern's metrics: relative L1 error per component, box-integrated drift of
-the conserved sums (run.py:186-187), and the kinetic-energy spectrum
-deviation.
+floor(|k| + 0.5). ``snapshot_fields`` restates the fields of
+jathenax/plot_snapshot.py:25-33 (tracer concentration, density and the
+centred-difference vorticity). Neither plots (matplotlib is not a
+dependency): ``python -m jathenax_gb300.diagnostics snapshot.npz`` writes the
+spectra CSV of spectra.py (``mode,kinetic_energy,enstrophy``) and the fields
+as an npz instead of figures. The error helpers are the Precision pattern's
+metrics: relative L1 error per component, box-integrated drift of the
+conserved sums (run.py:186-187), and the kinetic-energy spectrum deviation.
 """
+
+import argparse
+from pathlib import Path
 
 import numpy as np
 
@@ -37,6 +44,22 @@ def shell_spectra(U):
     enstrophy = np.bincount(shell.ravel(), (0.5 * np.abs(omega / rho.size)**2).ravel(),
                             minlength=len(modes))
     return modes, energy, enstrophy
+
+
+def snapshot_fields(U, dx, dy):
+    """{"tracer" (4+ variables), "density", "vorticity"} of a state (plot_snapshot.py:25-33).
+
+    Vorticity is dvy/dx - dvx/dy by periodic centred differences.
+    """
+    U = np.asarray(U, dtype=np.float64)
+    rho, mx, my = np.moveaxis(U[..., :3], -1, 0)
+    vx, vy = mx / rho, my / rho
+    dvy_dx = (np.roll(vy, -1, axis=1) - np.roll(vy, 1, axis=1)) / (2 * dx)
+    dvx_dy = (np.roll(vx, -1, axis=0) - np.roll(vx, 1, axis=0)) / (2 * dy)
+    fields = {"density": rho, "vorticity": dvy_dx - dvx_dy}
+    if U.shape[-1] > 3:
+        fields["tracer"] = U[..., 3] / rho
+    return fields
 
 
 def relative_l1(a, b):
@@ -77,3 +100,30 @@ def precision_report(U32, U64, U0, dx, dy):
         "drift_fp64": [float(v) for v in drift64[:3]],
         "ke_spectrum_max_rel_dev": spectrum_deviation(U32, U64),
     }
+
+
+def main(argv=None):
+    parser = argparse.ArgumentParser(description="Spectra and fields of a run's npz output (no plots).")
+    parser.add_argument("snapshot", type=Path, help="npz written by jathenax_gb300.run")
+    parser.add_argument("--output", type=Path, help="Output stem (default: next to the snapshot)")
+    args = parser.parse_args(argv)
+    stem = args.output or args.snapshot.with_suffix("")
+    with np.load(args.snapshot) as snap:
+        x, y = snap["x"], snap["y"]
+        initial, final = (snap[key].astype(np.float64) for key in ("initial", "conserved"))
+    dx, dy = float(x[1] - x[0]), float(y[1] - y[0])
+    modes, energy, enstrophy = shell_spectra(final)
+    spectra = Path(f"{stem}_spectra.csv")
+    spectra.parent.mkdir(parents=True, exist_ok=True)
+    np.savetxt(spectra, np.column_stack((modes, energy, enstrophy)), delimiter=",",
+               header="mode,kinetic_energy,enstrophy", comments="", fmt=("%d", "%.16e", "%.16e"))
+    fields = Path(f"{stem}_fields.npz")
+    arrays = {f"{when}_{name}": value for when, U in (("initial", initial), ("final", final))
+              for name, value in snapshot_fields(U, dx, dy).items()}
+    np.savez(fields, x=x, y=y, **arrays)
+    print(spectra)
+    print(fields)
+
+
+if __name__ == "__main__":
+    main()

@@ -36,3 +36,34 @@ def test_precision_report_is_zero_for_identical_states():
     rep = precision_report(U, U, U, 1 / 16, 1 / 16)
     assert rep["l1_density"] == 0 and rep["l1_momentum"] == 0 and rep["ke_spectrum_max_rel_dev"] == 0
     np.testing.assert_array_equal(relative_l1(U + 1e-3, U)[0] > 0, True)
+
+
+def test_snapshot_vorticity_of_a_shear_and_a_rotation():
+    from jathenax_gb300.diagnostics import snapshot_fields
+    n = 64
+    c = (np.arange(n) + 0.5) / n - 0.5
+    X, Y = np.meshgrid(c, c)
+    # vx = sin(2 pi y): vorticity -dvx/dy = -2 pi cos(2 pi y) * sin(2 pi h)/(2 pi h) (centred difference)
+    U = np.stack((np.full((n, n), 2.0), 2.0 * np.sin(2 * np.pi * Y), np.zeros((n, n)), np.ones((n, n))), -1)
+    f = snapshot_fields(U, 1 / n, 1 / n)
+    h = 1 / n
+    np.testing.assert_allclose(f["vorticity"], -np.cos(2 * np.pi * Y) * np.sin(2 * np.pi * h) / h, atol=1e-12)
+    np.testing.assert_allclose(f["tracer"], 0.5)
+    np.testing.assert_allclose(f["density"], 2.0)
+    assert set(snapshot_fields(U[..., :3], h, h)) == {"density", "vorticity"}
+
+
+def test_diagnostics_command_writes_spectra_csv_and_fields(tmp_path):
+    from jathenax_gb300 import diagnostics
+    n = 16
+    c = (np.arange(n) + 0.5) / n - 0.5
+    X, Y = np.meshgrid(c, c)
+    U = np.stack((1 + 0.1 * np.sin(2 * np.pi * X), 0.3 * np.cos(2 * np.pi * Y), 0.2 * np.sin(2 * np.pi * X)), -1)
+    np.savez(tmp_path / "run.npz", x=c, y=c, initial=U, conserved=U, time=0.0, dt=0.1, cycle=0)
+    diagnostics.main([str(tmp_path / "run.npz")])
+    table = np.loadtxt(tmp_path / "run_spectra.csv", delimiter=",", skiprows=1)
+    modes, energy, enstrophy = diagnostics.shell_spectra(U)
+    np.testing.assert_array_equal(table[:, 0], modes)
+    np.testing.assert_allclose(table[:, 1], energy, rtol=1e-15)
+    with np.load(tmp_path / "run_fields.npz") as f:
+        assert {"final_density", "final_vorticity", "initial_vorticity"} <= set(f.files)

@@ -6,7 +6,8 @@ the same order; where they can still differ is the compiler's contraction of
 a multiply and an add into one FMA, which depends on how often a product is
 reused (with donor-cell edges the x and y Riemann problems of a cell share
 products). So the two kernels are compared at the step tolerance in float64
-(and 1e-5 of each component's largest magnitude in float32), over every
+(in float32: 1e-6 in L1 per component and 1e-3 of each component's largest
+magnitude pointwise), over every
 reconstruction and Riemann solver, the viscous, drag and SGS-stress terms,
 RK4's saved-register stages and ragged and tiny periodic grids (fewer cells
 than one strip or one tile); the marching kernel against itself is bitwise
@@ -45,7 +46,15 @@ def stepped(U0, dtype, tile, integrator="rk3", steps=1, dt=0.001, recon="ppm4", 
 
 
 def assert_close(a, b, what):
-    assert_rel(a, b, STEP_RTOL if a.dtype == np.float64 else 1e-5, what)
+    if a.dtype == np.float64:
+        assert_rel(a, b, STEP_RTOL, what)
+        return
+    # float32: a rounding-level difference may flip a limiter branch (PPMX's
+    # smooth-extremum test, WENO-Z's near-flat weights) in a cell or two of a
+    # noisy state, so the pointwise bound is looser than the grid average.
+    assert_rel(a, b, 1e-3, what)
+    l1 = np.abs(a.astype(np.float64) - b).mean(axis=(0, 1)) / np.abs(b.astype(np.float64)).mean(axis=(0, 1))
+    assert l1.max() <= 1e-6, f"{what}: L1 difference {l1.max():.2e}"
 
 
 def assert_bitwise(a, b, what):
