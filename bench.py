@@ -42,7 +42,7 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # profiles/; None until such a capture exists for the dtype.
 # DRAM bytes (read + write) of one RK3 stage-2 launch at 4096^2, from a one-pass
 # ncu capture of this benchmark (dram__bytes_read.sum + dram__bytes_write.sum).
-STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1.08e9 + 510.69e6) / 4096**2, "f32": (597.40e6 + 238.46e6) / 4096**2}
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1.08e9 + 510.85e6) / 4096**2, "f32": (597.66e6 + 238.68e6) / 4096**2}
 
 
 def parse_args():
@@ -451,7 +451,9 @@ def bench_serving(torch, n):
     for rate in (200.0, 1000.0):
         for label, dtype in (("mixed_80pct_fp32", None), ("all_fp32", "float32")):
             reqs = stream(rate)
-            stats = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype).run(reqs)
+            server = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype)
+            server.warmup()
+            stats = server.run(reqs)
             errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs)
                     if (dtype or q.dtype) == "float32"]
             out[f"{label}_rate{int(rate)}"] = {

@@ -95,6 +95,20 @@ def _device_state(problem, n):
     return U
 
 
+def warmup_requests(dtypes=("float32", "float64")):
+    """One tiny request per problem, reconstruction, Riemann solver and precision:
+    running them once loads every kernel a stream can use (CUDA loads kernels
+    lazily, at their first launch), so a server's first requests do not pay for it."""
+    out = []
+    for dtype in dtypes:
+        for problem in PROBLEMS:
+            for recon in RECONS:
+                for rsolver in SOLVERS:
+                    out.append(Request(rid=-1 - len(out), arrival=0.0, problem=problem, side=16, reconstruct=recon,
+                                       rsolver=rsolver, tlim=0.004, dtype=dtype, seed=1))
+    return out
+
+
 def build_solve(req, tile=None, clock=None, dtype=None):
     """The device-resident Solve of one request (the reference's problem set-ups, run.py:133-163).
 
@@ -151,6 +165,11 @@ class Server:
         self.keep_results = keep_results
         self.dtype = dtype  # serve every request in this precision (None: as requested)
         self.builder = builder or build_solve  # (request, tile, clock, dtype) -> Solve
+
+    def warmup(self):
+        """Serve :func:`warmup_requests` once (untimed) to load every kernel."""
+        dtypes = (self.dtype,) if self.dtype else ("float32", "float64")
+        self.run(warmup_requests(dtypes))
 
     def run(self, requests):
         """Serve `requests` (arrival-ordered or not); returns a stats dict.

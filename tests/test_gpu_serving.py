@@ -70,3 +70,11 @@ def test_replanning_every_tick_keeps_results_exact():
         alone = build_solve(r)
         alone.run(steps_per_sync=4)
         np.testing.assert_array_equal(r.result, alone.S.cpu().numpy(), err_msg=str(r))
+
+
+def test_warmup_touches_every_method_and_precision():
+    from jathenax_gb300.serve import Server, warmup_requests
+    reqs = warmup_requests()
+    assert len(reqs) == 2 * 3 * 5 * 3
+    stats = Server(budget_bytes=1e9).run(reqs)
+    assert stats["completed"] == len(reqs)
