@@ -227,17 +227,18 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
     torch.cuda.synchronize()
     stage_ms = ks.elapsed_time(ke) / reps
 
-    # End to end through the public API: pinned host state in, one cycle, state out.
+    # End to end through the public API: each step uploads a state from pinned
+    # host memory, advances it one cycle and downloads the result; the uploads
+    # and downloads of neighbouring steps overlap the cycles (advance_host_many).
     host_in = solve.S.cpu().pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
     e2e_steps = max(2, min(args.steps, 10))
-    solve.advance_host(host_in, host_out)
+    solve.advance_host_many([host_in] * 2, [host_out] * 2)
     torch.cuda.synchronize()
     barrier(world)
     es, ee = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     es.record()
-    for _ in range(e2e_steps):
-        solve.advance_host(host_in, host_out)
+    solve.advance_host_many([host_in] * e2e_steps, [host_out] * e2e_steps)
     ee.record()
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(es.elapsed_time(ee), world)

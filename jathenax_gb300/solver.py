@@ -233,6 +233,54 @@ class Solve:
             self.enqueue_step()
         out_host.copy_(self.S, non_blocking=True)
 
+    def advance_host_many(self, inputs, outputs, steps=1):
+        """advance_host over a sequence of independent host states, with each
+        state's upload and download overlapping the cycles of its neighbours.
+
+        inputs/outputs are sequences of pinned CPU tensors of the state's shape
+        and dtype. State k is uploaded into one of two device buffers on an
+        upload stream, advanced on the current stream (CFL partials from the
+        loaded state, then `steps` cycles, the clock and workspace shared as in
+        advance_host, so results equal calling advance_host on each state in
+        turn) and downloaded on a download stream. The current stream waits for
+        the last download; nothing is synchronised with the host.
+        """
+        t = _lib.torch()
+        if getattr(self, "_host_bufs", None) is None:
+            self._host_bufs = (t.empty_like(self.S), t.empty_like(self.S))
+            self._up, self._down = t.cuda.Stream(), t.cuda.Stream()
+        cur = t.cuda.current_stream()
+        free = [None, None]  # download of the buffer's previous state has finished
+        forcing = ctypes.byref(self.forcing.struct) if self.forcing is not None else None
+        handle = _lib.stream_handle()
+        for k, (U_host, out_host) in enumerate(zip(inputs, outputs)):
+            b = k % 2
+            buf = self._host_bufs[b]
+            if k == 0:
+                self._up.wait_stream(cur)  # earlier work on the buffers is ordered first
+            if free[b] is not None:
+                self._up.wait_event(free[b])
+            with t.cuda.stream(self._up):
+                buf.copy_(U_host, non_blocking=True)
+            loaded = t.cuda.Event()
+            loaded.record(self._up)
+            cur.wait_event(loaded)
+            _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(buf), _lib.ptr(self.ws),
+                      self.nbytes, handle)
+            for _ in range(steps):
+                _lib.call("jx_step", ctypes.byref(self.desc), _lib.ptr(buf), _lib.ptr(self.A), _lib.ptr(self.B),
+                          forcing, _lib.ptr(self.clock), _lib.ptr(self.ws), self.nbytes, handle)
+            stepped = t.cuda.Event()
+            stepped.record(cur)
+            self._down.wait_event(stepped)
+            with t.cuda.stream(self._down):
+                out_host.copy_(buf, non_blocking=True)
+            free[b] = t.cuda.Event()
+            free[b].record(self._down)
+        for event in free:
+            if event is not None:
+                cur.wait_event(event)
+
     def enqueue_stage(self, stage, U_in, V_in, U_out, V_out=None):
         """Enqueue one fused stage kernel alone (used to time the kernel in isolation)."""
         _lib.call("jx_stage", ctypes.byref(self.desc), int(stage), _lib.ptr(U_in), _lib.ptr(V_in),

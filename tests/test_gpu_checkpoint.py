@@ -83,3 +83,24 @@ def test_evolve_isothermal_checkpoints_and_resumes(tmp_path):
     U, t, _, c = evolve_isothermal(U0, *args, 20, resume=tmp_path / "run.npz")
     assert c == c_full == 20 and t == t_full
     np.testing.assert_array_equal(U, U_full)
+
+
+def test_overlapped_host_advance_equals_one_at_a_time():
+    """advance_host_many overlaps transfers with cycles; results must equal advance_host in turn."""
+    import torch
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from jathenax_gb300.solver import Solve
+    rng = np.random.default_rng(4)
+    base = kelvin_helmholtz_tanh(96, 80)
+    states = [torch.from_numpy(base * (1 + 0.01 * rng.standard_normal(base.shape))).pin_memory() for _ in range(5)]
+    a = Solve(base, 1 / 96, 1 / 80, 1.0, 1e-10, "rk3", 0.4, 10.0, 10**6)
+    b = Solve(base, 1 / 96, 1 / 80, 1.0, 1e-10, "rk3", 0.4, 10.0, 10**6)
+    outs_a = [torch.empty_like(x).pin_memory() for x in states]
+    outs_b = [torch.empty_like(x).pin_memory() for x in states]
+    for x, o in zip(states, outs_a):
+        a.advance_host(x, o, steps=2)
+    b.advance_host_many(states, outs_b, steps=2)
+    torch.cuda.synchronize()
+    for x, y in zip(outs_a, outs_b):
+        np.testing.assert_array_equal(x.numpy(), y.numpy())
+    assert a.state().cycle == b.state().cycle and a.state().time == b.state().time
