@@ -86,13 +86,21 @@ def barrier(world):
 
 
 def max_over_ranks(value, world):
+    """The largest of every rank's value (the slowest rank's time)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    device = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replicas_rate(cells_per_step, steps, ms, world):
+    """Whole-job cell-updates/s: every rank advances its own replica of
+    `cells_per_step` cells `steps` times; `ms` is the slowest rank's time."""
+    return world * cells_per_step * steps / (ms * 1e-3)
 
 
 # ---------------------------------------------------------------------------
@@ -211,7 +219,7 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
     barrier(world)
     ms = max_over_ranks(start.elapsed_time(end), world)
     cells = n * n
-    value = world * cells * args.steps / (ms * 1e-3)
+    value = replicas_rate(cells, args.steps, ms, world)
     state = solve.state()
 
     # The dominant kernel alone: stage 2 (blend form) reading A, pointwise S, writing B.
@@ -246,7 +254,7 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
     tx, ty, smem = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
     _lib.call("jx_tile_info", ctypes.byref(solve.desc), ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(smem))
     return dict(value=value, ms=ms, stage_ms=stage_ms, clocks=clock_info, solve_state=state, tile=(tx.value, ty.value),
-                e2e=dict(value=world * cells * e2e_steps / (e2e_ms * 1e-3), unit=METRIC,
+                e2e=dict(value=replicas_rate(cells, e2e_steps, e2e_ms, world), unit=METRIC,
                          h2d_bytes_per_step=state_bytes, d2h_bytes_per_step=state_bytes),
                 dt=state.dt)
 
@@ -282,7 +290,7 @@ def cpu_baseline_sample(n, steps, procs=None):
         # spawn: this process may already hold a CUDA context. A worker that
         # dies raises BrokenProcessPool here instead of hanging the pool.
         with ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as pool:
-            start_at = time.time() + 10.0  # every worker has imported NumPy by then
+            start_at = time.time() + 5.0  # every worker has imported NumPy by then
             elapsed = list(pool.map(_oracle_cycles, [n] * procs, [steps] * procs, [start_at] * procs))
     slowest = max(elapsed)
     return dict(value=procs * n * n * steps / slowest, unit=METRIC, cores=procs, kind="port",
