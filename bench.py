@@ -362,14 +362,14 @@ def bench_ours(args, world, rank, local):
                    "parallelism": f"replicas x{world}"},
         "roofline": roofline(r64, w64, fp64_peak, "f64"),
         "e2e": r64["e2e"],
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 4 * args.steps,  # per step: begin-step + 3 stage kernels
         "clocks": r64["clocks"],
     }
     if r32 is not None:
         line["fp32"] = {"value": round(r32["value"], 1), "unit": METRIC,
                         "ms_per_step": round(r32["ms"] / args.steps, 4), "dtype": "f32",
-                        "roofline": roofline(r32, 4, fp32_peak, "f32"), "e2e": r32["e2e"]}
-        line["gpu_launches"] += 4 * args.steps
+                        "roofline": roofline(r32, 4, fp32_peak, "f32"), "e2e": r32["e2e"],
+                        "gpu_launches": 4 * args.steps}
     if rank == 0 and world == 1 and args.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
     if rank == 0 and world == 1 and not args.no_patterns:
