@@ -238,8 +238,9 @@ class Solve:
         state's upload and download overlapping the cycles of its neighbours.
 
         inputs/outputs are sequences of pinned CPU tensors of the state's shape
-        and dtype. State k is uploaded into one of two device buffers on an
-        upload stream, advanced on the current stream (CFL partials from the
+        and dtype. State k is uploaded into one of three device buffers (so the
+        upload of state k+1 and the download of state k-1 run at the same
+        time) on an upload stream, advanced on the current stream (CFL partials from the
         loaded state, then `steps` cycles, the clock and workspace shared as in
         advance_host, so results equal calling advance_host on each state in
         turn) and downloaded on a download stream. The current stream waits for
@@ -247,14 +248,15 @@ class Solve:
         """
         t = _lib.torch()
         if getattr(self, "_host_bufs", None) is None:
-            self._host_bufs = (t.empty_like(self.S), t.empty_like(self.S))
+            self._host_bufs = tuple(t.empty_like(self.S) for _ in range(3))
             self._up, self._down = t.cuda.Stream(), t.cuda.Stream()
         cur = t.cuda.current_stream()
-        free = [None, None]  # download of the buffer's previous state has finished
+        nbuf = len(self._host_bufs)
+        free = [None] * nbuf  # download of the buffer's previous state has finished
         forcing = ctypes.byref(self.forcing.struct) if self.forcing is not None else None
         handle = _lib.stream_handle()
         for k, (U_host, out_host) in enumerate(zip(inputs, outputs)):
-            b = k % 2
+            b = k % nbuf
             buf = self._host_bufs[b]
             if k == 0:
                 self._up.wait_stream(cur)  # earlier work on the buffers is ordered first
