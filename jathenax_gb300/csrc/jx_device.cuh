@@ -302,6 +302,18 @@ __device__ __forceinline__ void wenoz_cell(R m2, R m1, R c, R p1, R p2, R& lo, R
   lo = wenoz_combine(p2, p1, c, m1, m2, w2, w1, w0);
 }
 
+// RK stage combine of one component (hydro.py:39-51): the blend form
+// V + g0 (U - V) - beta dt div, else g0 U + g1 V - beta dt div, with
+// div = dFx/dx + dFy/dy. The flux differences enter through fused
+// multiply-adds with ncx = -beta dt/dx and ncy = -beta dt/dy (per launch),
+// which saves two float64 operations per component against forming div first.
+// Zero flux differences leave the blend form exact (U = V gives V).
+template <typename R>
+__device__ __forceinline__ R rk_combine(bool blend, R g0, R g1, R u, R v, R dfx, R dfy, R ncx, R ncy) {
+  const R base = blend ? fma(g0, u - v, v) : fma(g0, u, g1 * v);
+  return fma(ncy, dfy, fma(ncx, dfx, base));
+}
+
 // Face value shared by the two cells at a face (PPM4/PPMX only).
 template <int RECON, typename R>
 __device__ __forceinline__ R face_value(R w0, R w1, R w2, R w3) {
@@ -389,7 +401,6 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R ql = dl * tl, qr = dr * tr;
   const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
   const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
-  const R a0 = R(0.5) * (l0 + r0), a1 = R(0.5) * (l1 + r1), a2 = R(0.5) * (l2 + r2);
   // Roe averages (sl v_l + sr v_r) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
   // multiplied through by sl: (dl v_l + r v_r) / (dl + r), r = sqrt(dl dr).
   const R r = N::geo_mean(dl, dr);
@@ -398,25 +409,27 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R t = fma(r, tr, ql) * inv;
   const R lm = u - g.cs, lp = u + g.cs;
   const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
-  const R hu = (R(0.5) * u) * g.inv_cs;
+  const R hu = u * g.half_inv_cs;  // (u / 2) / cs
   const R jmc = jm * g.half_inv_cs;
   const R am = jd * (R(0.5) + hu) - jmc;
   const R az = jd * (-t) + jq;
   const R ap = jd * (R(0.5) - hu) + jmc;
-  const R km = R(-0.5) * fabs(lm) * am;
-  const R kz = R(-0.5) * fabs(u) * az;
-  const R kp = R(-0.5) * fabs(lp) * ap;
-  R g0 = a0 + km + kp;
-  R g1 = a1 + km * lm + kp * lp;
-  R g2 = a2 + km * t + kz + kp * t;
+  // g = (l + r)/2 - (|lm| am e_m + |u| az e_z + |lp| ap e_p)/2 with the
+  // eigenvectors e_m = (1, lm, t), e_z = (0, 0, 1), e_p = (1, lp, t).
+  const R wm = fabs(lm) * am, wz = fabs(u) * az, wp = fabs(lp) * ap;
+  const R wmp = wm + wp;
+  const R s0 = l0 + r0, s1 = l1 + r1, s2 = l2 + r2;
+  R g0 = R(0.5) * (s0 - wmp);
+  R g1 = R(0.5) * (s1 - fma(wm, lm, wp * lp));
+  R g2 = R(0.5) * (s2 - fma(wmp, t, wz));
   if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
   if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
   const R dstar = dl + am;
   if (N::lt0(dstar) || N::lt0(dstar + ap)) {
     const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
-    g0 = a0 - sp * jd;
-    g1 = a1 - sp * jm;
-    g2 = a2 - sp * jq;
+    g0 = R(0.5) * s0 - sp * jd;
+    g1 = R(0.5) * s1 - sp * jm;
+    g2 = R(0.5) * s2 - sp * jq;
   }
   f0 = g0;
   f1 = g1;

@@ -271,6 +271,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
   R* Vo = static_cast<R*>(p.Vout);
   const R sdt = s_sdt;
   const R kdrag = sdt * k.drag;
+  const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   R vmax0 = R(0), vmax1 = R(0);
   for (int idx = tid; idx < th * tw; idx += kStageThreads) {
     const int r = idx / tw, c = idx - r * tw;
@@ -281,7 +282,6 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
     for (int v = 0; v < NV; ++v) {
       const int fx = v * t.fxplane + r * (TX + 1) + c;
       const int fy = v * t.fyplane + r * TX + c;
-      const R div = (t.Fx[fx + 1] - t.Fx[fx]) * k.inv_dx + (t.Fy[fy + TX] - t.Fy[fy]) * k.inv_dy;
       const R u = v == 0 ? rho_in : U[cell + v];
       R vs = V[cell + v];
       if (v == 0 && p.floor_v) vs = N::lt(vs, k.dfloor) ? k.dfloor : vs;
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
         vs = vs + k.delta * u;
         if (Vo) Vo[cell + v] = vs;
       }
-      R un = p.blend ? vs + (k.g0 * (u - vs) - sdt * div) : k.g0 * u + k.g1 * vs - sdt * div;
+      R un = rk_combine<R>(p.blend, k.g0, k.g1, u, vs, t.Fx[fx + 1] - t.Fx[fx], t.Fy[fy + TX] - t.Fy[fy], ncx, ncy);
       if (p.drag_on && (v == 1 || v == 2)) un = un + -((kdrag * rho_in) * t.W[v * t.wplane + sw]);
       if (p.trace_on) {
         if (p.trace.saved) static_cast<R*>(p.trace.saved)[cell + v] = vs;

@@ -304,6 +304,7 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
   R* Vo = static_cast<R*>(p.Vout);
   const R sdt = *s_sdt;
   const R kdrag = sdt * k.drag;
+  const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   R vmax0 = R(0), vmax1 = R(0);
   for (int idx = tid; idx < TY * TX; idx += kStageThreads) {
     const int r = idx / TX, c = idx - r * TX;
@@ -319,10 +320,9 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
     Cell4<R> un;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const R div = (fxr.v[v] - fxl.v[v]) * k.inv_dx + (fyr.v[v] - fyl.v[v]) * k.inv_dy;
       if (p.has_delta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
-      un.v[v] = p.blend ? vs.v[v] + (k.g0 * (u.v[v] - vs.v[v]) - sdt * div)
-                        : k.g0 * u.v[v] + k.g1 * vs.v[v] - sdt * div;
+      un.v[v] = rk_combine<R>(p.blend, k.g0, k.g1, u.v[v], vs.v[v], fxr.v[v] - fxl.v[v], fyr.v[v] - fyl.v[v], ncx,
+                              ncy);
     }
     un.v[3] = NV == 4 ? un.v[3] : R(0);
     if (p.drag_on) {

@@ -165,6 +165,7 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   gas.half_inv_cs = k.half_inv_cs;
   const R sdt = static_cast<R>(p.beta * p.clock->dt);
   const R kdrag = sdt * k.drag;
+  const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   constexpr unsigned kAll = 0xffffffffu;
 
   MarchColumn<R> col[2];
@@ -297,10 +298,9 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
           Cell4<R> un;
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
-            const R div = (fr.v[v] - fl.v[v]) * k.inv_dx + (Fy2[h].v[v] - col[h].Fy3.v[v]) * k.inv_dy;
             if (p.has_delta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
-            un.v[v] = p.blend ? vs.v[v] + (k.g0 * (u.v[v] - vs.v[v]) - sdt * div)
-                              : k.g0 * u.v[v] + k.g1 * vs.v[v] - sdt * div;
+            un.v[v] = rk_combine<R>(p.blend, k.g0, k.g1, u.v[v], vs.v[v], fr.v[v] - fl.v[v],
+                                    Fy2[h].v[v] - col[h].Fy3.v[v], ncx, ncy);
           }
           un.v[3] = NV == 4 ? un.v[3] : R(0);
           if (p.drag_on) {
