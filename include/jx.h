@@ -242,6 +242,16 @@ jx_status jx_viscous_flux(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, con
                           double dx, double dy, double viscosity, double smagorinsky_cs,
                           int32_t axis, void* out, jx_stream s);
 
+/* face_velocity_gradients (fluxes.py:227-238): dv_dx and dv_dy, each
+ * (ny, nx, 2) = both velocity components, at the low faces along axis
+ * (1 = x, 0 = y), from primitives W (ny, nx, nv). */
+jx_status jx_face_velocity_gradients(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, const void* W, double dx,
+                                     double dy, int32_t axis, void* dv_dx, void* dv_dy, jx_stream s);
+/* smagorinsky_viscosity (fluxes.py:241-245): Cs^2 dx dy sqrt(2 S:S) per
+ * face from the gradients above; out has ncell values. */
+jx_status jx_smagorinsky_viscosity(int32_t dtype, int64_t ncell, const void* dv_dx, const void* dv_dy, double dx,
+                                   double dy, double smagorinsky_cs, void* out, jx_stream s);
+
 /* Sum of (rho, rho*vx, rho*vy, ...) over the grid in float64 (the
  * box-integrated conservation check of run.py:186-187). out: nvar doubles. */
 jx_status jx_box_sums(const jx_desc* d, const void* U, double* out, void* workspace,

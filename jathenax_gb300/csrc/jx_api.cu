@@ -657,6 +657,24 @@ jx_status jx_viscous_flux(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, con
                     "viscous-flux kernel");
 }
 
+jx_status jx_face_velocity_gradients(int32_t dtype, int32_t ny, int32_t nx, int32_t nv, const void* W, double dx,
+                                     double dy, int32_t axis, void* dv_dx, void* dv_dy, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (axis != 0 && axis != 1) return fail(JX_ERR_INVALID, "axis must be 0 (y) or 1 (x)");
+  if (ny < 0 || nx < 0 || nv < 3) return fail(JX_ERR_INVALID, "bad shape");
+  if ((int64_t)ny * nx > 0 && (!W || !dv_dx || !dv_dy)) return fail(JX_ERR_INVALID, "null array");
+  return cuda_check(launch_face_gradients(dtype, ny, nx, nv, W, dx, dy, axis, dv_dx, dv_dy, (cudaStream_t)s),
+                    "face-gradient kernel");
+}
+
+jx_status jx_smagorinsky_viscosity(int32_t dtype, int64_t ncell, const void* dv_dx, const void* dv_dy, double dx,
+                                   double dy, double smagorinsky_cs, void* out, jx_stream s) {
+  if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
+  if (ncell < 0 || (ncell > 0 && (!dv_dx || !dv_dy || !out))) return fail(JX_ERR_INVALID, "bad arguments");
+  const double c = smagorinsky_cs * smagorinsky_cs * dx * dy;
+  return cuda_check(launch_smagorinsky(dtype, ncell, dv_dx, dv_dy, c, out, (cudaStream_t)s), "Smagorinsky kernel");
+}
+
 jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sink, jx_stream s) {
   if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
   if (blocks < 1 || iters < 1 || !sink) return fail(JX_ERR_INVALID, "bad probe arguments");

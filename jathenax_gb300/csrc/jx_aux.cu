@@ -631,6 +631,72 @@ cudaError_t launch_viscous_flux(int dtype, int ny, int nx, int nv, const void* W
   return cudaGetLastError();
 }
 
+// face_velocity_gradients (fluxes.py:227-238): (dv/dx, dv/dy) of both
+// velocity components at each cell's low face along axis (1 = x, 0 = y),
+// each (ny, nx, 2).
+template <typename R>
+__global__ void face_gradients_kernel(int ny, int nx, int nv, const R* W, R dx, R dy, int axis, R* gx, R* gy) {
+  const int64_t n = (int64_t)ny * nx;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int j = (int)(k / nx), i = (int)(k - (int64_t)j * nx);
+  auto w = [&](int jj, int ii, int c) -> R {
+    return W[((int64_t)wrap_index(jj, ny) * nx + wrap_index(ii, nx)) * nv + c];
+  };
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    R normal, trans;
+    if (axis == 1) {
+      normal = (w(j, i, c + 1) - w(j, i - 1, c + 1)) / dx;
+      trans = ((w(j + 1, i, c + 1) + w(j + 1, i - 1, c + 1)) - (w(j - 1, i, c + 1) + w(j - 1, i - 1, c + 1))) /
+              (R(4) * dy);
+      gx[k * 2 + c] = normal;
+      gy[k * 2 + c] = trans;
+    } else {
+      normal = (w(j, i, c + 1) - w(j - 1, i, c + 1)) / dy;
+      trans = ((w(j, i + 1, c + 1) + w(j - 1, i + 1, c + 1)) - (w(j, i - 1, c + 1) + w(j - 1, i - 1, c + 1))) /
+              (R(4) * dx);
+      gx[k * 2 + c] = trans;
+      gy[k * 2 + c] = normal;
+    }
+  }
+}
+
+// smagorinsky_viscosity (fluxes.py:241-245): Cs^2 dx dy sqrt(2 S:S), (ny, nx).
+template <typename R>
+__global__ void smagorinsky_kernel(int64_t n, const R* gx, const R* gy, R c, R* out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const R shear = gx[k * 2 + 1] + gy[k * 2 + 0];
+  const R s2 = R(2) * (gx[k * 2] * gx[k * 2] + gy[k * 2 + 1] * gy[k * 2 + 1]) + shear * shear;
+  out[k] = c * sqrt(s2);
+}
+
+cudaError_t launch_face_gradients(int dtype, int ny, int nx, int nv, const void* W, double dx, double dy, int axis,
+                                  void* gx, void* gy, cudaStream_t s) {
+  const int64_t n = (int64_t)ny * nx;
+  if (n == 0) return cudaSuccess;
+  const int g = (int)((n + 255) / 256);
+  if (dtype == JX_F64)
+    face_gradients_kernel<double><<<g, 256, 0, s>>>(ny, nx, nv, (const double*)W, dx, dy, axis, (double*)gx,
+                                                    (double*)gy);
+  else
+    face_gradients_kernel<float><<<g, 256, 0, s>>>(ny, nx, nv, (const float*)W, (float)dx, (float)dy, axis,
+                                                   (float*)gx, (float*)gy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smagorinsky(int dtype, int64_t n, const void* gx, const void* gy, double c, void* out,
+                               cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int g = (int)((n + 255) / 256);
+  if (dtype == JX_F64)
+    smagorinsky_kernel<double><<<g, 256, 0, s>>>(n, (const double*)gx, (const double*)gy, c, (double*)out);
+  else
+    smagorinsky_kernel<float><<<g, 256, 0, s>>>(n, (const float*)gx, (const float*)gy, (float)c, (float*)out);
+  return cudaGetLastError();
+}
+
 // Box sums of every component in float64 (fixed decomposition).
 template <typename R>
 __global__ void box_sum_kernel(const R* U, int64_t ncell, int nv, int64_t chunk, double* part) {

@@ -105,6 +105,32 @@ def _solver(name, rho_l, rho_r, vn_l, vn_r, vt_l, vt_r, cs):
 RIEMANN_SOLVERS = {name: partial(_solver, name) for name in ("llf", "hlle", "roe")}
 
 
+def face_velocity_gradients(W, dx, dy, axis):
+    """(dv/dx, dv/dy) of both velocity components at each low face along axis (fluxes.py:227-238)."""
+    Wd = _lib.to_device(W)
+    if Wd.ndim != 3 or Wd.shape[-1] < 3:
+        raise ValueError("expected W with shape (ny, nx, nvar >= 3)")
+    ny, nx, nv = Wd.shape
+    t = _lib.torch()
+    gx = t.empty((ny, nx, 2), dtype=Wd.dtype, device=Wd.device)
+    gy = t.empty((ny, nx, 2), dtype=Wd.dtype, device=Wd.device)
+    _lib.call("jx_face_velocity_gradients", _lib.dtype_id(Wd.dtype), ny, nx, nv, _lib.ptr(Wd), float(dx), float(dy),
+              int(axis), _lib.ptr(gx), _lib.ptr(gy), _lib.stream_handle())
+    return _lib.like_input(gx, W), _lib.like_input(gy, W)
+
+
+def smagorinsky_viscosity(dv_dx, dv_dy, dx, dy, smagorinsky_cs):
+    """Kinematic eddy viscosity (Cs sqrt(dx dy))^2 times the strain norm (fluxes.py:241-245)."""
+    gx = _lib.to_device(dv_dx)
+    gy = _lib.to_device(dv_dy, gx.dtype)
+    if gx.shape != gy.shape or gx.ndim != 3 or gx.shape[-1] != 2:
+        raise ValueError("expected two gradient arrays of shape (ny, nx, 2)")
+    out = _lib.torch().empty(tuple(gx.shape[:2]), dtype=gx.dtype, device=gx.device)
+    _lib.call("jx_smagorinsky_viscosity", _lib.dtype_id(gx.dtype), gx.shape[0] * gx.shape[1], _lib.ptr(gx),
+              _lib.ptr(gy), float(dx), float(dy), float(smagorinsky_cs), _lib.ptr(out), _lib.stream_handle())
+    return _lib.like_input(out, dv_dx)
+
+
 def viscous_momentum_flux(W, dx, dy, viscosity, smagorinsky_cs, axis):
     """Negative viscous (plus Smagorinsky) stress for the momentum fluxes (fluxes.py:248-266)."""
     Wd = _lib.to_device(W)

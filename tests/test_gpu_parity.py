@@ -235,6 +235,12 @@ def test_face_operators_match_oracle():
     for axis in (0, 1):
         assert_rel(GF.viscous_momentum_flux(W, 1 / 20, 1 / 14, 1e-3, 0.2, axis),
                    H.viscous_flux(W, 1 / 20, 1 / 14, 1e-3, 0.2, axis), STEP_RTOL)
+        gx, gy = GF.face_velocity_gradients(W, 1 / 20, 1 / 14, axis)
+        rx, ry = H.face_gradients(W, 1 / 20, 1 / 14, axis)
+        np.testing.assert_array_equal(gx, rx)
+        np.testing.assert_array_equal(gy, ry)
+        assert_rel(GF.smagorinsky_viscosity(gx, gy, 1 / 20, 1 / 14, 0.17)[..., None],
+                   H.eddy_viscosity(rx, ry, 1 / 20, 1 / 14, 0.17)[..., None], STEP_RTOL)
     tau = noisy_state(20, 14, nvar=3, seed=8)
     for a, b in zip(GF.stress_face_fluxes(tau), H.sgs_face_flux(tau)):
         assert_rel(a, b, STEP_RTOL)
