@@ -1023,9 +1023,9 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
       off_render[next_off] = F.render_work;
       off_sum[next_off] = F.sum_work;
       off_kick[next_off] = F.kick_work;
-      F.render_work += render_blocks(ncell);
+      F.render_work += render_blocks(d.ny, d.nx);
       F.sum_work += fq[nf].nblk;
-      F.kick_work += cfl_grid(ncell);
+      F.kick_work += kick_blocks(ncell);
       ++next_off;
       ++nf;
       ++F.count;

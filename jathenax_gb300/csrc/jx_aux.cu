@@ -136,14 +136,15 @@ __global__ void cfl_kernel(CflParams q) {
   const R inv_dx = static_cast<R>(q.inv_dx), inv_dy = static_cast<R>(q.inv_dy);
   const R inv_4dx = static_cast<R>(q.inv_4dx), inv_4dy = static_cast<R>(q.inv_4dy);
   const int64_t n = (int64_t)q.ny * q.nx;
-  double v[3] = {0.0, 0.0, 0.0};
+  // Maxima in the state precision, widened once per block (exact).
+  R v[3] = {R(0), R(0), R(0)};
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / q.nx), i = (int)(k - (int64_t)j * q.nx);
     R rho, vx, vy;
     velocity_at<R, FROM_W>(X, q.nx, q.nv, dfloor, j, i, rho, vx, vy);
-    v[0] = nan_max(v[0], static_cast<double>(fabs(vx) + cs));
-    v[1] = nan_max(v[1], static_cast<double>(fabs(vy) + cs));
+    v[0] = nan_max(v[0], fabs(vx) + cs);
+    v[1] = nan_max(v[1], fabs(vy) + cs);
     if (q.smag) {
       const int jm = wrap_index(j - 1, q.ny), jp = wrap_index(j + 1, q.ny);
       const int im = wrap_index(i - 1, q.nx), ip = wrap_index(i + 1, q.nx);
@@ -161,7 +162,7 @@ __global__ void cfl_kernel(CflParams q) {
         const R dvy_dy = ((uy[1] + uy[2]) - (uy[3] + uy[4])) * inv_4dy;
         const R sh = dvy_dx + dvx_dy;
         const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + sh * sh;
-        v[2] = nan_max(v[2], static_cast<double>(s2));
+        v[2] = nan_max(v[2], s2);
       }
       // y face (low face of cell j): needs (j, i+1), (j-1, i+1) as well
       velocity_at<R, FROM_W>(X, q.nx, q.nv, dfloor, j, ip, r_, ux[5], uy[5]);
@@ -173,16 +174,16 @@ __global__ void cfl_kernel(CflParams q) {
         const R dvy_dx = ((uy[5] + uy6) - (uy[0] + uy[4])) * inv_4dx;
         const R sh = dvy_dx + dvx_dy;
         const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + sh * sh;
-        v[2] = nan_max(v[2], static_cast<double>(s2));
+        v[2] = nan_max(v[2], s2);
       }
     }
   }
-  block_nan_max<3>(v, red);
+  block_nan_max<3>(v, reinterpret_cast<R*>(red));
   if (threadIdx.x == 0) {
     double* out = q.partials + (size_t)blockIdx.x * kCflSlots;
-    out[0] = v[0];
-    out[1] = v[1];
-    out[2] = v[2];
+    out[0] = static_cast<double>(v[0]);
+    out[1] = static_cast<double>(v[1]);
+    out[2] = static_cast<double>(v[2]);
     if (blockIdx.x == 0) q.header->n_cfl = gridDim.x;
   }
 }
@@ -195,35 +196,140 @@ __global__ void cfl_kernel(CflParams q) {
 // blockIdx.x and gridDim.x, the batched kernels (one launch for every forced
 // solve of a batch) the position of the block in the solve's own range, so a
 // solve's sums are bitwise the same alone and in a batch.
+// The raw field is separable per mode: with a = cos(kx x), b = sin(kx x),
+// c = cos(ky y), d = sin(ky y) and amplitudes (a00, a01, a10, a11),
+//   re*a00 - im*a01 = a*(c*a00 - d*a01) - b*(d*a00 + c*a01)
+// (re = ac - bd, im = ad + bc), and likewise for the second component. A
+// block renders a kRenderCols x kRenderRows tile: it forms the four row
+// coefficients of its rows for a chunk of modes in shared memory (amplitudes
+// widened or narrowed to the state precision once per block), then each
+// thread adds 4 FMAs per mode per cell for its column and rows. NaN
+// amplitudes (an update row past the table) give a NaN field, as before.
+constexpr int kRenderCols = 32, kRenderRows = 32, kRenderModes = 8;
+constexpr int kRenderRowsPerThread = kRenderRows / (kReduceThreads / 32);
+static_assert(kRenderRows * kRenderModes == kReduceThreads, "one row coefficient per thread per chunk");
+
 template <typename R>
 __device__ __forceinline__ void render_body(const RenderParams& q, int b) {
+  __shared__ R amp[kRenderModes * 4];
+  __shared__ __align__(16) R rowc[kRenderRows][kRenderModes][4];
   if (q.clock->done || !q.clock->render) return;
-  const int64_t n = (int64_t)q.ny * q.nx;
-  const int64_t k = (int64_t)b * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const int j = (int)(k / q.nx), i = (int)(k - (int64_t)j * q.nx);
+  const int tiles_x = (q.nx + kRenderCols - 1) / kRenderCols;
+  const int ty = b / tiles_x;
+  const int i0 = (b - ty * tiles_x) * kRenderCols, j0 = ty * kRenderRows;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = min(i0 + lane, q.nx - 1);  // loads clamp; stores check
   const R* cx = static_cast<const R*>(q.cos_x);
   const R* sx = static_cast<const R*>(q.sin_x);
   const R* cy = static_cast<const R*>(q.cos_y);
   const R* sy = static_cast<const R*>(q.sin_y);
   const int row = q.clock->update;
   const bool valid = row >= 0 && row < q.n_updates;  // .at[].get(mode="fill") -> NaN
-  const double* amp = q.table + (size_t)(valid ? row : 0) * q.n_modes * 4;
-  R f0 = R(0), f1 = R(0);
-  for (int m = 0; m < q.n_modes; ++m) {
-    const R a = cx[(size_t)m * q.nx + i], b2 = sx[(size_t)m * q.nx + i];
-    const R c = cy[(size_t)m * q.ny + j], d = sy[(size_t)m * q.ny + j];
-    const R re = a * c - b2 * d;
-    const R im = a * d + b2 * c;
-    R a00 = static_cast<R>(amp[m * 4 + 0]), a01 = static_cast<R>(amp[m * 4 + 1]);
-    R a10 = static_cast<R>(amp[m * 4 + 2]), a11 = static_cast<R>(amp[m * 4 + 3]);
-    if (!valid) a00 = a01 = a10 = a11 = static_cast<R>(NAN);
-    f0 = f0 + (re * a00 - im * a01);
-    f1 = f1 + (re * a10 - im * a11);
+  const double* table = q.table + (size_t)(valid ? row : 0) * q.n_modes * 4;
+  // The coefficient this thread forms in each chunk: row er, mode em.
+  const int er = threadIdx.x / kRenderModes, em = threadIdx.x - er * kRenderModes;
+  const int ej = min(j0 + er, q.ny - 1);
+  R f0[kRenderRowsPerThread], f1[kRenderRowsPerThread];
+#pragma unroll
+  for (int t = 0; t < kRenderRowsPerThread; ++t) f0[t] = f1[t] = R(0);
+  for (int m0 = 0; m0 < q.n_modes; m0 += kRenderModes) {
+    const int mc = min(kRenderModes, q.n_modes - m0);
+    __syncthreads();  // the previous chunk's coefficients are consumed
+    if (threadIdx.x < mc * 4) amp[threadIdx.x] = valid ? static_cast<R>(table[m0 * 4 + threadIdx.x]) : static_cast<R>(NAN);
+    __syncthreads();
+    if (em < mc) {
+      const size_t at = (size_t)(m0 + em) * q.ny + ej;
+      const R c = cy[at], d = sy[at];
+      const R a00 = amp[em * 4 + 0], a01 = amp[em * 4 + 1], a10 = amp[em * 4 + 2], a11 = amp[em * 4 + 3];
+      rowc[er][em][0] = c * a00 - d * a01;
+      rowc[er][em][1] = d * a00 + c * a01;
+      rowc[er][em][2] = c * a10 - d * a11;
+      rowc[er][em][3] = d * a10 + c * a11;
+    }
+    __syncthreads();
+    for (int mm = 0; mm < mc; ++mm) {
+      const size_t at = (size_t)(m0 + mm) * q.nx + i;
+      const R a = cx[at], nb = -sx[at];
+#pragma unroll
+      for (int t = 0; t < kRenderRowsPerThread; ++t) {
+        const R* k = rowc[warp + t * (kReduceThreads / 32)][mm];
+        f0[t] = fma(nb, k[1], fma(a, k[0], f0[t]));
+        f1[t] = fma(nb, k[3], fma(a, k[2], f1[t]));
+      }
+    }
   }
+  if (i0 + lane >= q.nx) return;
   R* F = static_cast<R*>(q.raw);
-  F[k * 2 + 0] = f0;
-  F[k * 2 + 1] = f1;
+#pragma unroll
+  for (int t = 0; t < kRenderRowsPerThread; ++t) {
+    const int j = j0 + warp + t * (kReduceThreads / 32);
+    if (j >= q.ny) break;
+    const int64_t k = (int64_t)j * q.nx + i0 + lane;
+    F[k * 2 + 0] = f0[t];
+    F[k * 2 + 1] = f1[t];
+  }
+}
+
+// Per-thread accumulation of a solve's grid sums. A float64 state adds each
+// term in float64. A float32 state sums its float32 terms in float32 with
+// Knuth's TwoSum error-free transformation: the pair (s, c) carries the
+// running sum to about twice float32's precision, warps reduce the pairs the
+// same way and widen to float64 once per warp, so the float64 pipe (a small
+// fraction of the float32 rate on this part) sees a few operations per warp
+// instead of a conversion and an add per term. The explicit _rn intrinsics
+// keep the compiler from contracting or reassociating the transformation.
+template <typename R> struct GridSum;
+template <> struct GridSum<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct GridSum<float> {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    const float xb = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, xb)), __fsub_rn(x, xb));
+    s = t;
+    c = __fadd_rn(c, e);
+  }
+  __device__ __forceinline__ double value() const { return static_cast<double>(s) + static_cast<double>(c); }
+  // Fixed butterfly over the warp: TwoSum of the two partners' s (exact, so
+  // its error term does not depend on which partner is first) and the sum of
+  // their c.
+  __device__ __forceinline__ void warp_reduce() {
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+      add(so);
+      c = __fadd_rn(c, co);
+    }
+  }
+};
+
+// Block total of K per-thread sums, valid in thread 0: a float32 state
+// reduces each warp in (s, c) pairs and widens once per warp; a float64
+// state reduces in float64 (block_sum's fixed order).
+template <int K, typename R>
+__device__ __forceinline__ void block_grid_sum(GridSum<R> (&a)[K], double (&v)[K], double* red /* 32*K */) {
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = a[k].value();
+    block_sum<K>(v, red);
+  } else {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) a[k].warp_reduce();
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) red[warp * K + k] = a[k].value();
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = warp_sum(lane < nwarp ? red[lane * K + k] : 0.0);
+    }
+  }
 }
 
 // Pass 1: block partials of sum(rho), sum(rho*Fx), sum(rho*Fy).
@@ -234,14 +340,15 @@ __device__ __forceinline__ void sum1_body(const ForceParams& q, int b, double* r
   const R* F = static_cast<const R*>(q.raw);
   const int64_t n = (int64_t)q.ny * q.nx;
   const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
-  double v[3] = {0.0, 0.0, 0.0};
+  GridSum<R> a[3];
   for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
     const R rho = U[k * q.nv];
-    v[0] += static_cast<double>(rho);
-    v[1] += static_cast<double>(rho * F[2 * k]);
-    v[2] += static_cast<double>(rho * F[2 * k + 1]);
+    a[0].add(rho);
+    a[1].add(rho * F[2 * k]);
+    a[2].add(rho * F[2 * k + 1]);
   }
-  block_sum<3>(v, red);
+  double v[3];
+  block_grid_sum<3>(a, v, red);
   if (threadIdx.x == 0) {
     double* out = q.p1 + (size_t)b * 4;
     out[0] = v[0];
@@ -276,15 +383,16 @@ __device__ __forceinline__ void sum2_body(const ForceParams& q, int b, double* r
   const R dt = static_cast<R>(q.clock->dt);
   const int64_t n = (int64_t)q.ny * q.nx;
   const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
-  double v[2] = {0.0, 0.0};
+  GridSum<R> a[2];
   for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
     const R* u = U + k * q.nv;
     const R fx = F[2 * k] - mx, fy = F[2 * k + 1] - my;
     const R f2 = fx * fx + fy * fy;
-    v[0] += static_cast<double>(R(0.5) * u[0] * f2 * dt);
-    v[1] += static_cast<double>(u[1] * fx + u[2] * fy);
+    a[0].add(R(0.5) * u[0] * f2 * dt);
+    a[1].add(u[1] * fx + u[2] * fy);
   }
-  block_sum<2>(v, red);
+  double v[2];
+  block_grid_sum<2>(a, v, red);
   if (threadIdx.x == 0) {
     q.p2[(size_t)b * 4 + 0] = v[0];
     q.p2[(size_t)b * 4 + 1] = v[1];
@@ -329,7 +437,10 @@ __device__ __forceinline__ void kick_body(const ForceParams& q, int b, int nb, d
   R* accel = static_cast<R*>(q.acceleration);
   R* after = static_cast<R*>(q.conserved);
   const int64_t n = (int64_t)q.ny * q.nx;
-  double v[2] = {0.0, 0.0};
+  // CFL maxima in the state precision, reduced over the block and widened
+  // once: the max commutes with the exact, monotone widening, so the float64
+  // partials are unchanged.
+  R c0 = R(0), c1 = R(0);
   for (int64_t k = (int64_t)b * blockDim.x + threadIdx.x; k < n; k += (int64_t)nb * blockDim.x) {
     R* u = U + k * q.nv;
     if (before)
@@ -358,16 +469,17 @@ __device__ __forceinline__ void kick_body(const ForceParams& q, int b, int nb, d
     u[2] = m2;
     if (q.want_cfl) {
       const R inv = Num<R>::rcp(rf);
-      v[0] = nan_max(v[0], static_cast<double>(fabs(inv * m1) + cs));
-      v[1] = nan_max(v[1], static_cast<double>(fabs(inv * m2) + cs));
+      c0 = nan_max(c0, fabs(inv * m1) + cs);
+      c1 = nan_max(c1, fabs(inv * m2) + cs);
     }
   }
   if (q.want_cfl) {
-    block_nan_max<2>(v, red);
+    R v[2] = {c0, c1};
+    block_nan_max<2>(v, reinterpret_cast<R*>(red));
     if (threadIdx.x == 0) {
       double* out = q.partials + (size_t)b * kCflSlots;
-      out[0] = v[0];
-      out[1] = v[1];
+      out[0] = static_cast<double>(v[0]);
+      out[1] = static_cast<double>(v[1]);
       out[2] = 0.0;
       if (b == 0) q.header->n_cfl = nb;
     }
@@ -777,7 +889,7 @@ cudaError_t launch_cfl(int dtype, bool from_w, const CflParams& q, cudaStream_t 
 }
 
 cudaError_t launch_render(int dtype, const RenderParams& q, cudaStream_t s) {
-  const int g = render_blocks((int64_t)q.ny * q.nx);
+  const int g = render_blocks(q.ny, q.nx);
   if (dtype == JX_F64) render_kernel<double><<<g, kReduceThreads, 0, s>>>(q);
   else render_kernel<float><<<g, kReduceThreads, 0, s>>>(q);
   return cudaGetLastError();
@@ -791,8 +903,13 @@ void force_decomposition(int64_t ncell, int* nblk, int64_t* chunk) {
   *chunk = (ncell + b - 1) / b;
 }
 
+int kick_blocks(int64_t ncell) {
+  int64_t g = (ncell + kKickCellsPerBlock - 1) / kKickCellsPerBlock;
+  return (int)(g < 1 ? 1 : (g > kCflBlocksMax ? kCflBlocksMax : g));
+}
+
 cudaError_t launch_force_kick(int dtype, const ForceParams& q, cudaStream_t s) {
-  const int g = cfl_grid((int64_t)q.ny * q.nx);
+  const int g = kick_blocks((int64_t)q.ny * q.nx);
   if (dtype == JX_F64) force_sum1_kernel<double><<<q.nblk, kReduceThreads, 0, s>>>(q);
   else force_sum1_kernel<float><<<q.nblk, kReduceThreads, 0, s>>>(q);
   force_fin1_kernel<<<1, kReduceThreads, 0, s>>>(q);
@@ -804,7 +921,9 @@ cudaError_t launch_force_kick(int dtype, const ForceParams& q, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-int render_blocks(int64_t ncell) { return (int)((ncell + kReduceThreads - 1) / kReduceThreads); }
+int render_blocks(int ny, int nx) {
+  return ((nx + kRenderCols - 1) / kRenderCols) * ((ny + kRenderRows - 1) / kRenderRows);
+}
 
 cudaError_t launch_render_batch(int dtype, const RenderParams* q, const int* off, int n, int nwork, cudaStream_t s) {
   if (n < 1 || nwork < 1) return cudaSuccess;

@@ -62,9 +62,13 @@ cudaError_t launch_render(int dtype, const RenderParams& q, cudaStream_t s);
 void force_decomposition(int64_t ncell, int* nblk, int64_t* chunk);
 cudaError_t launch_force_kick(int dtype, const ForceParams& q, cudaStream_t s);
 // Batched forcing over n solves of one precision: render blocks, pass-1/2
-// blocks (force_decomposition's nblk) and kick blocks (cfl_grid) per solve
+// blocks (force_decomposition's nblk) and kick blocks (kick_blocks) per solve
 // are laid end to end; off[i] is solve i's first block, off[n] the total.
-int render_blocks(int64_t ncell);
+int render_blocks(int ny, int nx);
+// Kick grid: kKickCellsPerBlock cells per block (8 per thread), at most
+// kCflBlocksMax blocks (the CFL partial slots).
+constexpr int kKickCellsPerBlock = 8 * kReduceThreads;
+int kick_blocks(int64_t ncell);
 cudaError_t launch_render_batch(int dtype, const RenderParams* q, const int* off, int n, int nwork, cudaStream_t s);
 cudaError_t launch_force_kick_batch(int dtype, const ForceParams* q, int n, const int* off_sum, int sum_work,
                                     const int* off_kick, int kick_work, cudaStream_t s);

@@ -447,7 +447,10 @@ __device__ __forceinline__ void riemann(R dl, R dr, R ul, R ur, R tl, R tr, cons
 // ---------------------------------------------------------------------------
 // Reductions.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_nan_max(double v) {
+// Max reductions are exact, so reducing in float32 and widening the result
+// gives the same float64 value as widening every input first.
+template <typename T>
+__device__ __forceinline__ T warp_nan_max(T v) {
   for (int o = 16; o > 0; o >>= 1) v = nan_max(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
@@ -459,8 +462,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Block-wide NaN-propagating max of K values; result valid in thread 0.
-template <int K>
-__device__ __forceinline__ void block_nan_max(double (&v)[K], double* scratch /* 32*K */) {
+template <int K, typename T>
+__device__ __forceinline__ void block_nan_max(T (&v)[K], T* scratch /* 32*K */) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) v[k] = warp_nan_max(v[k]);
@@ -473,7 +476,7 @@ __device__ __forceinline__ void block_nan_max(double (&v)[K], double* scratch /*
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      double x = lane < nwarp ? scratch[lane * K + k] : 0.0;
+      T x = lane < nwarp ? scratch[lane * K + k] : T(0);
       v[k] = warp_nan_max(x);
     }
   }
