@@ -207,6 +207,7 @@ __global__ void cfl_kernel(CflParams q) {
 // amplitudes (an update row past the table) give a NaN field, as before.
 constexpr int kRenderCols = 32, kRenderRows = 32, kRenderModes = 8;
 constexpr int kRenderRowsPerThread = kRenderRows / (kReduceThreads / 32);
+constexpr int kRenderBatchBlocks = 152 * 8;  // batched render grid (8 blocks per SM)
 static_assert(kRenderRows * kRenderModes == kReduceThreads, "one row coefficient per thread per chunk");
 
 template <typename R>
@@ -532,9 +533,13 @@ __device__ __forceinline__ int batch_solve_of(const int* __restrict__ off, int n
 }
 
 template <typename R>
-__global__ void render_batch_kernel(const RenderParams* __restrict__ q, const int* __restrict__ off, int n) {
-  const int i = batch_solve_of(off, n, blockIdx.x);
-  render_body<R>(q[i], blockIdx.x - off[i]);
+__global__ void render_batch_kernel(const RenderParams* __restrict__ q, const int* __restrict__ off, int n, int nwork) {
+  // Grid-stride over the tiles: most cycles render nothing, and a small grid
+  // makes that cheap; a tile's result does not depend on which block takes it.
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int i = batch_solve_of(off, n, w);
+    render_body<R>(q[i], w - off[i]);
+  }
 }
 
 template <typename R>
@@ -927,8 +932,9 @@ int render_blocks(int ny, int nx) {
 
 cudaError_t launch_render_batch(int dtype, const RenderParams* q, const int* off, int n, int nwork, cudaStream_t s) {
   if (n < 1 || nwork < 1) return cudaSuccess;
-  if (dtype == JX_F64) render_batch_kernel<double><<<nwork, kReduceThreads, 0, s>>>(q, off, n);
-  else render_batch_kernel<float><<<nwork, kReduceThreads, 0, s>>>(q, off, n);
+  const int g = nwork < kRenderBatchBlocks ? nwork : kRenderBatchBlocks;
+  if (dtype == JX_F64) render_batch_kernel<double><<<g, kReduceThreads, 0, s>>>(q, off, n, nwork);
+  else render_batch_kernel<float><<<g, kReduceThreads, 0, s>>>(q, off, n, nwork);
   return cudaGetLastError();
 }
 
