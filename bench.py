@@ -59,6 +59,19 @@ def parse_args():
     p.add_argument("--no-patterns", action="store_true",
                    help="skip the batched / serving / precision measurements")
     p.add_argument("--serve-requests", type=int, default=100)
+    p.add_argument("--turbulence-t", type=float, default=None,
+                   help="instead of the benchmark line: the driven-turbulence configuration on the --n "
+                        "grid (default 1024 here) to this end time in float32 and float64, with the "
+                        "precision report (L1 error, drift, KE spectrum deviation)")
+    p.add_argument("--cs", type=float, default=0.0, help="Smagorinsky constant for --turbulence-t")
+    p.add_argument("--average-from", type=float, default=None,
+                   help="with --turbulence-t: also compare KE spectra averaged over t = T0, T0+1, ..., end")
+    p.add_argument("--chaos-floor", action="store_true",
+                   help="with --turbulence-t: add a float64 run from a 1e-12-perturbed density")
+    p.add_argument("--ensemble", choices=("all", "kh", "turbulence"), default=None,
+                   help="instead of the benchmark line: time --steps batched cycles (after --warmup) of "
+                        "the 64-solve float32 ensemble (or its KH / turbulence half) at --tile")
+    p.add_argument("--tile", default="58x32", help="tile of --ensemble, e.g. 58x32 or 32x16")
     p.add_argument("--sweep", action="store_true",
                    help="instead of the benchmark line: one JSON line per reconstruction x Riemann "
                         "solver x integrator x precision on the --n grid (default 1024 here)")
@@ -521,6 +534,101 @@ def bench_precision(torch):
     return out
 
 
+def bench_ensemble(args):
+    """Batched cycles of the 64-solve ensemble (or one half) at one tile: one JSON line."""
+    import torch
+    from jathenax_gb300.batch import Batch
+    from jathenax_gb300.serve import build_solve
+    torch.cuda.set_device(0)
+    tile = tuple(int(v) for v in args.tile.lower().split("x"))
+    reqs = [make_request(k, n, s, 1.0, "float32", i) for i, (k, n, s) in enumerate(ensemble_specs())
+            if args.ensemble == "all" or k == args.ensemble]
+    batch = Batch([build_solve(r, tile) for r in reqs])
+    for _ in range(args.warmup):
+        batch.enqueue_step()
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    start.record(stream)
+    for _ in range(args.steps):
+        batch.enqueue_step()
+    end.record(stream)
+    end.synchronize()
+    cells = sum(r.side * r.side for r in reqs)
+    ms = start.elapsed_time(end) / max(args.steps, 1)
+    print(json.dumps({"workload": f"{len(reqs)} float32 solves ({args.ensemble}) of the 64-solve ensemble, "
+                                  f"ppm4+roe rk3, tile {tile[0]}x{tile[1]}",
+                      "cells": cells, "steps": args.steps, "warmup": args.warmup, "ms_per_cycle": round(ms, 4),
+                      "cell_updates_per_s": round(cells / ms * 1e3, 1)}), flush=True)
+
+
+def bench_turbulence_long(args):
+    """The driven-turbulence configuration to a long end time in both precisions (one JSON line).
+
+    With ``--average-from T0`` the KE shell spectrum is also averaged over the
+    snapshots at T0, T0 + 1, ..., tlim (each run stops exactly at those times)
+    and compared as time averages. With ``--chaos-floor`` a third, float64 run
+    starts from the same state with the density perturbed by 1e-12 (relative,
+    seeded noise): its distance from the float64 run is the chaotic
+    divergence that no precision can remove, the scale the float32 numbers are
+    read against.
+    """
+    import torch
+    from jathenax_gb300.diagnostics import precision_report, shell_spectra
+    torch.cuda.set_device(0)
+    side = args.n or 1024
+    tlim = args.turbulence_t
+    samples = [] if args.average_from is None else \
+        [float(t) for t in np.arange(args.average_from, tlim + 0.5, 1.0) if t <= tlim]
+    runs = [("float32", "float32", 0.0), ("float64", "float64", 0.0)]
+    if args.chaos_floor:
+        runs.append(("float64_perturbed", "float64", 1e-12))
+    res, info, spectra = {}, {}, {}
+    U0 = None
+    for name, dtype, eps in runs:
+        s = driven_turbulence(side, tlim, dtype, smagorinsky_cs=args.cs)
+        if U0 is None:
+            U0 = s.S.cpu().numpy().astype(np.float64)
+        if eps:
+            noise = np.random.default_rng(45).standard_normal(U0.shape[:2])
+            s.S[..., 0] *= torch.as_tensor(1.0 + eps * noise, device=s.S.device, dtype=s.S.dtype)
+        acc = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for stop in samples + [tlim]:
+            s.set_clock(tlim=stop, done=0)
+            s.run(steps_per_sync=256)
+            if stop in samples:
+                acc.append(shell_spectra(s.S.cpu().numpy())[1])
+        torch.cuda.synchronize()
+        seconds = time.perf_counter() - t0
+        state = s.state()
+        res[name] = s.S.cpu().numpy()
+        if acc:
+            spectra[name] = np.mean(acc, axis=0)
+        info[name] = {"cycles": state.cycle, "time": state.time, "seconds": round(seconds, 2),
+                      "cell_updates_per_s": round(side * side * state.cycle / seconds, 1)}
+        del s
+
+    def mean_spectrum_dev(a, b, kmax):
+        sl = slice(1, kmax)
+        return float(np.max(np.abs(spectra[a][sl] - spectra[b][sl]) / np.maximum(spectra[b][sl], 1e-300)))
+
+    out = {"workload": f"driven turbulence {side}^2, rk3 ppm4 roe, seed 1618, nu 1.5e-6, drag 0.3333335, "
+                       f"Cs {args.cs}, t={tlim}",
+           "precision": precision_report(res["float32"], res["float64"], U0, 1 / side, 1 / side), "runs": info}
+    if args.chaos_floor:
+        out["chaos_floor"] = precision_report(res["float64_perturbed"], res["float64"], U0, 1 / side, 1 / side)
+    if spectra:
+        out["time_averaged_spectrum"] = {"times": samples}
+        for name in spectra:
+            if name == "float64":
+                continue
+            out["time_averaged_spectrum"][f"{name}_vs_float64"] = {
+                f"max_rel_dev_k<{k}": mean_spectrum_dev(name, "float64", k) for k in (16, 64, side // 2)}
+    print(json.dumps(out), flush=True)
+
+
 def bench_reference(args, world, rank):
     """The reference algorithm's CPU path (the float64 oracle port) on host cores."""
     if rank != 0:
@@ -578,6 +686,12 @@ def main():
     args = parse_args()
     if args.sweep:
         bench_sweep(args)
+        return
+    if args.turbulence_t is not None:
+        bench_turbulence_long(args)
+        return
+    if args.ensemble is not None:
+        bench_ensemble(args)
         return
     args.n = args.n or 4096
     world, rank, local = dist_setup(args)

@@ -534,11 +534,31 @@ __device__ __forceinline__ int batch_solve_of(const int* __restrict__ off, int n
 
 template <typename R>
 __global__ void render_batch_kernel(const RenderParams* __restrict__ q, const int* __restrict__ off, int n, int nwork) {
-  // Grid-stride over the tiles: most cycles render nothing, and a small grid
-  // makes that cheap; a tile's result does not depend on which block takes it.
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const int i = batch_solve_of(off, n, w);
-    render_body<R>(q[i], w - off[i]);
+  // Block b owns tiles b, b + G, b + 2G, ... (G = gridDim.x). Most cycles
+  // render nothing, so the block first tests up to kReduceThreads of its
+  // tiles at once (one thread each: find the solve, read its clock), lists
+  // the ones whose solve renders this cycle, then renders the list. A tile's
+  // result does not depend on which block takes it or in which order.
+  __shared__ int todo[kReduceThreads];
+  __shared__ int count;
+  const int G = gridDim.x;
+  for (int base = blockIdx.x; base < nwork; base += G * kReduceThreads) {
+    if (threadIdx.x == 0) count = 0;
+    __syncthreads();
+    const int w = base + threadIdx.x * G;
+    if (w < nwork) {
+      const int i = batch_solve_of(off, n, w);
+      const jx_clock* c = q[i].clock;
+      if (!c->done && c->render) todo[atomicAdd(&count, 1)] = w;
+    }
+    __syncthreads();
+    const int m = count;
+    for (int t = 0; t < m; ++t) {
+      const int wt = todo[t];
+      const int i = batch_solve_of(off, n, wt);
+      render_body<R>(q[i], wt - off[i]);
+    }
+    __syncthreads();  // todo and count are rewritten by the next round
   }
 }
 
