@@ -143,20 +143,21 @@ template <> struct Num<double> {
     const long long e = (bits(x) >> 52) & 0x7ff;  // biased exponent
     return e < 24 || e > 2000;
   }
-  // 1/x by Newton-Raphson refinement of the special-function unit's seed
-  // (PTX rcp.approx.ftz.f64): each step y <- y + y (1 - x y) squares the
-  // relative error (Flynn, "On division by functional iteration", IEEE TC
-  // 1970); two steps take the seed to within about an ulp of 1/x (checked
-  // against correctly rounded division by the tests). Four DFMA instead of
-  // the longer correctly rounded sequence; float64 parity allows the ulp.
+  // 1/x refined from the special-function unit's seed y (PTX
+  // rcp.approx.ftz.f64) by one third-order step of the series
+  // 1/x = y / (1 - e) = y (1 + e + e^2 + ...), e = 1 - x y:
+  // y <- y + y (e + e^2), which cubes the seed's relative error (Flynn, "On
+  // division by functional iteration", IEEE TC 1970) — from the seed's
+  // ~2^-23 to far below an ulp, leaving the final rounding: within an ulp of
+  // 1/x (checked against correctly rounded division by the tests). Three
+  // DFMA instead of the longer correctly rounded sequence; float64 parity
+  // allows the ulp.
   static __device__ __forceinline__ double rcp(double x) {
     if (outside_seed_range(x)) return 1.0 / x;
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double r = fma(-x, y, 1.0);
-    y = fma(y, r, y);
-    r = fma(-x, y, 1.0);
-    return fma(y, r, y);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
   }
   static __device__ __forceinline__ double root(double x) { return sqrt(x); }
   // sqrt(a) sqrt(b) for a, b >= 0 with one square root, sqrt(a b), unless

@@ -1,7 +1,7 @@
 """The stage kernels' reciprocal, quotient and Roe square-root product
 (Num<R>::rcp/div/geo_mean) against correctly rounded NumPy arithmetic.
 
-The float64 reciprocal is a Newton-Raphson refinement of the special-function
+The float64 reciprocal is a third-order refinement of the special-function
 unit's seed and must stay within 1 ulp of the correctly rounded result over
 the whole seeded range, with IEEE results (inf, NaN, subnormal handling)
 outside it; the float64 quotient is correctly rounded; float32 uses the
