@@ -1,11 +1,11 @@
 """The stage kernels' reciprocal, quotient and Roe square-root product
 (Num<R>::rcp/div/geo_mean) against correctly rounded NumPy arithmetic.
 
-The float64 reciprocal is a third-order refinement of the special-function
-unit's seed and must stay within 1 ulp of the correctly rounded result over
-the whole seeded range, with IEEE results (inf, NaN, subnormal handling)
-outside it; the float64 quotient is correctly rounded; float32 uses the
-unit's approximations and must stay within 2-3 ulp.
+The float64 reciprocal and square root are third-order refinements of the
+special-function unit's seeds and must stay within 1 ulp of the correctly
+rounded results over the whole seeded range, with IEEE results (inf, NaN,
+subnormal handling) outside it; the float64 quotient is correctly rounded;
+float32 uses the unit's approximations and must stay within 2-3 ulp.
 """
 
 import ctypes
@@ -47,6 +47,18 @@ def test_float64_reciprocal_and_quotient_within_one_ulp():
         np.testing.assert_array_equal(div, a / b)
     ref = np.sqrt(np.abs(a)) * np.sqrt(np.abs(b))
     assert ulps(geo, ref).max() <= 2.0
+
+
+def test_float64_square_root_within_one_ulp():
+    # geo_mean(p, 1) is the refined square root of p inside the seed's range
+    # and the correctly rounded one outside it.
+    rng = np.random.default_rng(3)
+    p = np.concatenate([np.abs(wide(rng, 400000, np.float64, -990, 970)), rng.uniform(0.25, 4.0, 100000),
+                        2.0 ** np.arange(-1020, 1020, dtype=np.float64), [0.0, np.inf, np.finfo(np.float64).tiny]])
+    _, _, geo = probe(p, np.ones_like(p))
+    finite = np.isfinite(p) & (p > 0)
+    assert ulps(geo[finite], np.sqrt(p[finite])).max() <= 1.0
+    np.testing.assert_array_equal(geo[~finite], np.sqrt(p[~finite]))
 
 
 def test_float64_edges_take_ieee_arithmetic():
