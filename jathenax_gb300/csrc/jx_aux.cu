@@ -676,6 +676,7 @@ __global__ void face_flux_kernel(int64_t nface, int nv, int axis, const R* L, co
   g.cs2 = static_cast<R>(cs * cs);
   g.inv_cs = static_cast<R>(1.0 / cs);
   g.half_inv_cs = static_cast<R>(0.5 / cs);
+  g.quarter_inv_cs = static_cast<R>(0.25 / cs);
   const R* l = L + k * nv;
   const R* r = Rr + k * nv;
   const int nn = axis == 1 ? 1 : 2, tt = axis == 1 ? 2 : 1;

@@ -22,10 +22,10 @@
 // WENO-Z weights, CFL speeds) go through Num<R>::rcp/div. In float32 both use
 // the special-function unit's approximations (PTX rcp.approx.f32,
 // sqrt.approx.f32, about one unit in the last place). In float64 the
-// reciprocals of the recovery, the Riemann solvers and the CFL speeds are a
-// Newton-Raphson refinement of the unit's float64 seed (within an ulp; the
-// tolerance against the reference is 1e-12 per stage), and quotients stay
-// correctly rounded.
+// reciprocals of the recovery, the Riemann solvers and the CFL speeds, and
+// the square root of the Roe/HLLE average, are third-order refinements of
+// the unit's float64 seeds (within an ulp; the tolerance against the
+// reference is 1e-12 per stage), and quotients stay correctly rounded.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -367,7 +367,7 @@ __device__ __forceinline__ void edges_from_stencil(R m3, R m2, R m1, R c, R p1, 
 // Riemann solvers in the (normal, tangential) frame (fluxes.py:134-201).
 // ---------------------------------------------------------------------------
 template <typename R> struct Gas {
-  R cs, cs2, inv_cs, half_inv_cs;
+  R cs, cs2, inv_cs, half_inv_cs, quarter_inv_cs;
 };
 
 template <typename R>
@@ -425,23 +425,45 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R t = fma(r, tr, ql) * inv;
   const R lm = u - g.cs, lp = u + g.cs;
   const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
-  const R hu = u * g.half_inv_cs;  // (u / 2) / cs
-  const R jmc = jm * g.half_inv_cs;
-  const R am = jd * (R(0.5) + hu) - jmc;
-  const R az = jd * (-t) + jq;
-  const R ap = jd * (R(0.5) - hu) + jmc;
+  // Wave strengths am = jd (1/2 + u/(2cs)) - jm/(2cs), az = jq - jd t,
+  // ap = jd (1/2 - u/(2cs)) + jm/(2cs);
   // g = (l + r)/2 - (|lm| am e_m + |u| az e_z + |lp| ap e_p)/2 with the
   // eigenvectors e_m = (1, lm, t), e_z = (0, 0, 1), e_p = (1, lp, t).
-  const R wm = fabs(lm) * am, wz = fabs(u) * az, wp = fabs(lp) * ap;
-  const R wmp = wm + wp;
+  // In float64 am, ap and |u| az are formed halved (every input scaled by
+  // 1/2, so the halves are exact) and each component is one FMA: bit for bit
+  // the halved difference, two float64 operations fewer per face. Float32
+  // keeps the unhalved form, which measured faster in the marching kernel.
   const R s0 = l0 + r0, s1 = l1 + r1, s2 = l2 + r2;
-  R g0 = R(0.5) * (s0 - wmp);
-  R g1 = R(0.5) * (s1 - fma(wm, lm, wp * lp));
-  R g2 = R(0.5) * (s2 - fma(wmp, t, wz));
+  const R az = fma(jd, -t, jq);
+  R g0, g1, g2, dstar, dstar2;
+  if constexpr (sizeof(R) == 8) {
+    const R hq = u * g.quarter_inv_cs;  // (u / 4) / cs
+    const R jmq = jm * g.quarter_inv_cs;
+    const R am = fma(jd, R(0.25) + hq, -jmq);  // am / 2
+    const R ap = fma(jd, R(0.25) - hq, jmq);   // ap / 2
+    const R wm = fabs(lm) * am, wz = (R(0.5) * fabs(u)) * az, wp = fabs(lp) * ap;  // halves
+    const R wmp = wm + wp;
+    g0 = fma(R(0.5), s0, -wmp);
+    g1 = fma(R(0.5), s1, -fma(wm, lm, wp * lp));
+    g2 = fma(R(0.5), s2, -fma(wmp, t, wz));
+    dstar = fma(R(2), am, dl);  // dl + am
+    dstar2 = fma(R(2), ap, dstar);
+  } else {
+    const R hu = u * g.half_inv_cs;  // (u / 2) / cs
+    const R jmc = jm * g.half_inv_cs;
+    const R am = fma(jd, R(0.5) + hu, -jmc);
+    const R ap = fma(jd, R(0.5) - hu, jmc);
+    const R wm = fabs(lm) * am, wz = fabs(u) * az, wp = fabs(lp) * ap;
+    const R wmp = wm + wp;
+    g0 = R(0.5) * (s0 - wmp);
+    g1 = R(0.5) * (s1 - fma(wm, lm, wp * lp));
+    g2 = R(0.5) * (s2 - fma(wmp, t, wz));
+    dstar = dl + am;
+    dstar2 = dstar + ap;
+  }
   if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
   if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
-  const R dstar = dl + am;
-  if (N::lt0(dstar) || N::lt0(dstar + ap)) {
+  if (N::lt0(dstar) || N::lt0(dstar2)) {
     const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
     g0 = R(0.5) * s0 - sp * jd;
     g1 = R(0.5) * s1 - sp * jm;

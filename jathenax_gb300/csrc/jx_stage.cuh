@@ -121,6 +121,7 @@ __device__ __forceinline__ void sweep(const StageParams& p, const StageConsts<R>
     gas.cs2 = k.cs2;
     gas.inv_cs = k.inv_cs;
     gas.half_inv_cs = k.half_inv_cs;
+    gas.quarter_inv_cs = R(0.5) * k.half_inv_cs;
     const R* __restrict__ tau = static_cast<const R*>(p.tau);
     const int len = n + 1;  // faces 0 .. n
     constexpr int nn = DIR == 0 ? 1 : 2, tt = DIR == 0 ? 2 : 1;

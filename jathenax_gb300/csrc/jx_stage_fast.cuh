@@ -175,6 +175,7 @@ __device__ __forceinline__ void fast_sweep(const StageParams& p, const StageCons
     gas.cs2 = k.cs2;
     gas.inv_cs = k.inv_cs;
     gas.half_inv_cs = k.half_inv_cs;
+    gas.quarter_inv_cs = R(0.5) * k.half_inv_cs;
     const R* __restrict__ tau = static_cast<const R*>(p.tau);
     constexpr int nn = DIR == 0 ? 1 : 2, tt = DIR == 0 ? 2 : 1;
     const int total = DIR == 0 ? TY * (TX + 1) : (TY + 1) * TX;  // faces 0 .. n

@@ -168,6 +168,7 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   gas.cs2 = k.cs2;
   gas.inv_cs = k.inv_cs;
   gas.half_inv_cs = k.half_inv_cs;
+  gas.quarter_inv_cs = R(0.5) * k.half_inv_cs;
   const R sdt = static_cast<R>(p.beta * p.clock->dt);
   const R kdrag = sdt * k.drag;
   const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
