@@ -219,10 +219,20 @@ __device__ __forceinline__ void ppm4_cell(R c, R lo_face, R hi_face, R& lo, R& h
   const R dh = hi_face - c;
   const R dl = lo_face - c;
   const bool flat = N::prod_ge0(dh, dl);
-  const R l2 = N::abs_ge_twice(dl, dh) ? c - R(2) * dh : lo_face;
-  const R h2 = N::abs_ge_twice(dh, dl) ? c - R(2) * dl : hi_face;
-  lo = flat ? c : l2;
-  hi = flat ? c : h2;
+  const bool steep_lo = N::abs_ge_twice(dl, dh), steep_hi = N::abs_ge_twice(dh, dl);
+  if constexpr (sizeof(R) == 8) {
+    // The two steepening tests hold together only for dl = dh = 0, which is
+    // flat: one FMA, on the selected difference, serves whichever applies
+    // (one float64 operation fewer per variable and direction).
+    const R x = c - R(2) * (steep_lo ? dh : dl);
+    lo = flat ? c : (steep_lo ? x : lo_face);
+    hi = flat ? c : (steep_hi ? x : hi_face);
+  } else {
+    const R l2 = steep_lo ? c - R(2) * dh : lo_face;
+    const R h2 = steep_hi ? c - R(2) * dl : hi_face;
+    lo = flat ? c : l2;
+    hi = flat ? c : h2;
+  }
 }
 
 // Smooth-extremum limiter of one face value (fluxes.py:45-53).
@@ -265,8 +275,18 @@ __device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face
   const bool use = agree && N::pgt(fabs(d2), R(1e-12) * scale);
   R ratio = R(0);
   if (use) ratio = N::div(lim, d2);
-  const R lm = N::abs_ge_twice(dl, dh) ? c - R(2) * dh : lo_face;
-  const R hm = N::abs_ge_twice(dh, dl) ? c - R(2) * dl : hi_face;
+  const bool steep_lo = N::abs_ge_twice(dl, dh), steep_hi = N::abs_ge_twice(dh, dl);
+  R lm, hm;
+  if constexpr (sizeof(R) == 8) {
+    // As in ppm4_cell: both tests hold only for dl = dh = 0, where both
+    // results are c, so one FMA serves whichever applies.
+    const R x = c - R(2) * (steep_lo ? dh : dl);
+    lm = steep_lo ? x : lo_face;
+    hm = steep_hi ? x : hi_face;
+  } else {
+    lm = steep_lo ? c - R(2) * dh : lo_face;
+    hm = steep_hi ? c - R(2) * dl : hi_face;
+  }
   lo = ext ? c + dl * ratio : lm;
   hi = ext ? c + dh * ratio : hm;
 }
