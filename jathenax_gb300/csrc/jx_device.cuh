@@ -37,6 +37,9 @@ template <typename R> struct Tiny;
 template <> struct Tiny<double> { static constexpr double value = 2.2250738585072014e-308; };
 template <> struct Tiny<float> { static constexpr float value = 1.17549435e-38f; };
 
+// A compile-time boolean for dispatching a runtime flag once per kernel.
+template <bool B> struct Flag { static constexpr bool value = B; };
+
 // NaN-propagating max/min (jnp.maximum/minimum and the max/min reductions).
 template <typename T> __device__ __forceinline__ T nan_max(T a, T b) {
   return (a > b || a != a) ? a : b;

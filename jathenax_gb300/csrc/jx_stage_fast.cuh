@@ -307,42 +307,56 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
   const R kdrag = sdt * k.drag;
   const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   R vmax0 = R(0), vmax1 = R(0);
-  for (int idx = tid; idx < TY * TX; idx += kStageThreads) {
-    const int r = idx / TX, c = idx - r * TX;
-    if (y0 + r >= p.ny || x0 + c >= p.nx) continue;
-    const size_t cell = (size_t)(y0 + r) * p.nx + (x0 + c);
-    const Cell4<R> w = t.W[(r + H) * PW + (c + H)];
-    const Cell4<R> fxl = t.Fx[r * (TX + 1) + c], fxr = t.Fx[r * (TX + 1) + c + 1];
-    const Cell4<R> fyl = t.Fy[r * TX + c], fyr = t.Fy[(r + 1) * TX + c];
-    Cell4<R> u = load_cell<R, NV>(U + cell * NV);
-    u.v[0] = w.v[0];  // the floored density
-    Cell4<R> vs = load_cell<R, NV>(V + cell * NV);
-    if (p.floor_v) vs.v[0] = N::lt(vs.v[0], k.dfloor) ? k.dfloor : vs.v[0];
-    Cell4<R> un;
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      if (p.has_delta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
-      un.v[v] = rk_combine<R>(p.blend, k.g0, k.g1, u.v[v], vs.v[v], fxr.v[v] - fxl.v[v], fyr.v[v] - fyl.v[v], ncx,
-                              ncy);
+  // The combine loop is instantiated per (blend form, RK4 delta, drag) so
+  // that no float64 work of an unused form is evaluated and then discarded.
+  auto combine = [&](auto blend_tag, auto delta_tag, auto drag_tag) {
+    constexpr bool kBlend = decltype(blend_tag)::value;
+    constexpr bool kDelta = decltype(delta_tag)::value;
+    constexpr bool kDrag = decltype(drag_tag)::value;
+    for (int idx = tid; idx < TY * TX; idx += kStageThreads) {
+      const int r = idx / TX, c = idx - r * TX;
+      if (y0 + r >= p.ny || x0 + c >= p.nx) continue;
+      const size_t cell = (size_t)(y0 + r) * p.nx + (x0 + c);
+      const Cell4<R> w = t.W[(r + H) * PW + (c + H)];
+      const Cell4<R> fxl = t.Fx[r * (TX + 1) + c], fxr = t.Fx[r * (TX + 1) + c + 1];
+      const Cell4<R> fyl = t.Fy[r * TX + c], fyr = t.Fy[(r + 1) * TX + c];
+      Cell4<R> u = load_cell<R, NV>(U + cell * NV);
+      u.v[0] = w.v[0];  // the floored density
+      Cell4<R> vs = load_cell<R, NV>(V + cell * NV);
+      if (p.floor_v) vs.v[0] = N::lt(vs.v[0], k.dfloor) ? k.dfloor : vs.v[0];
+      Cell4<R> un;
+  #pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        if (kDelta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
+        un.v[v] = rk_combine<R>(kBlend, k.g0, k.g1, u.v[v], vs.v[v], fxr.v[v] - fxl.v[v], fyr.v[v] - fyl.v[v], ncx,
+                                ncy);
+      }
+      un.v[3] = NV == 4 ? un.v[3] : R(0);
+      if (kDrag) {
+        un.v[1] = un.v[1] + -((kdrag * w.v[0]) * w.v[1]);
+        un.v[2] = un.v[2] + -((kdrag * w.v[0]) * w.v[2]);
+      }
+      if (p.trace_on) {
+        store_cell_scalar<R, NV>(p.trace.saved, cell, vs);
+        store_cell_scalar<R, NV>(p.trace.conserved, cell, un);
+        store_cell_scalar<R, NV>(p.trace.primitives, cell, w);
+      }
+      if (kDelta && Vo) store_cell<R, NV>(Vo + cell * NV, vs);
+      if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
+      store_cell<R, NV>(Uo + cell * NV, un);
+      if (p.want_cfl) {
+        const R inv = Num<R>::rcp(un.v[0]);
+        vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
+        vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
+      }
     }
-    un.v[3] = NV == 4 ? un.v[3] : R(0);
-    if (p.drag_on) {
-      un.v[1] = un.v[1] + -((kdrag * w.v[0]) * w.v[1]);
-      un.v[2] = un.v[2] + -((kdrag * w.v[0]) * w.v[2]);
-    }
-    if (p.trace_on) {
-      store_cell_scalar<R, NV>(p.trace.saved, cell, vs);
-      store_cell_scalar<R, NV>(p.trace.conserved, cell, un);
-      store_cell_scalar<R, NV>(p.trace.primitives, cell, w);
-    }
-    if (p.has_delta && Vo) store_cell<R, NV>(Vo + cell * NV, vs);
-    if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
-    store_cell<R, NV>(Uo + cell * NV, un);
-    if (p.want_cfl) {
-      const R inv = Num<R>::rcp(un.v[0]);
-      vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
-      vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
-    }
+  };
+  if (p.blend) {
+    if (p.has_delta) p.drag_on ? combine(Flag<true>{}, Flag<true>{}, Flag<true>{}) : combine(Flag<true>{}, Flag<true>{}, Flag<false>{});
+    else p.drag_on ? combine(Flag<true>{}, Flag<false>{}, Flag<true>{}) : combine(Flag<true>{}, Flag<false>{}, Flag<false>{});
+  } else {
+    if (p.has_delta) p.drag_on ? combine(Flag<false>{}, Flag<true>{}, Flag<true>{}) : combine(Flag<false>{}, Flag<true>{}, Flag<false>{});
+    else p.drag_on ? combine(Flag<false>{}, Flag<false>{}, Flag<true>{}) : combine(Flag<false>{}, Flag<false>{}, Flag<false>{});
   }
   if (p.want_cfl) {
     double vmax[2] = {static_cast<double>(vmax0), static_cast<double>(vmax1)};
