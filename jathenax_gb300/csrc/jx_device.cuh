@@ -486,7 +486,7 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   }
   if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
   if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
-  if (N::lt0(dstar) || N::lt0(dstar2)) {
+  if (__builtin_expect(N::lt0(dstar) || N::lt0(dstar2), 0)) {  // positivity fix: rare
     const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
     g0 = R(0.5) * s0 - sp * jd;
     g1 = R(0.5) * s1 - sp * jm;

@@ -307,12 +307,14 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
   const R kdrag = sdt * k.drag;
   const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   R vmax0 = R(0), vmax1 = R(0);
-  // The combine loop is instantiated per (blend form, RK4 delta, drag) so
-  // that no float64 work of an unused form is evaluated and then discarded.
-  auto combine = [&](auto blend_tag, auto delta_tag, auto drag_tag) {
+  // The combine loop is instantiated per (blend form, RK4 delta, drag, CFL
+  // partials) so that no float64 work of an unused form is evaluated and
+  // then discarded.
+  auto combine = [&](auto blend_tag, auto delta_tag, auto drag_tag, auto cfl_tag) {
     constexpr bool kBlend = decltype(blend_tag)::value;
     constexpr bool kDelta = decltype(delta_tag)::value;
     constexpr bool kDrag = decltype(drag_tag)::value;
+    constexpr bool kCfl = decltype(cfl_tag)::value;
     for (int idx = tid; idx < TY * TX; idx += kStageThreads) {
       const int r = idx / TX, c = idx - r * TX;
       if (y0 + r >= p.ny || x0 + c >= p.nx) continue;
@@ -344,20 +346,27 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
       if (kDelta && Vo) store_cell<R, NV>(Vo + cell * NV, vs);
       if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
       store_cell<R, NV>(Uo + cell * NV, un);
-      if (p.want_cfl) {
+      if (kCfl) {
         const R inv = Num<R>::rcp(un.v[0]);
         vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
         vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
       }
     }
   };
-  if (p.blend) {
-    if (p.has_delta) p.drag_on ? combine(Flag<true>{}, Flag<true>{}, Flag<true>{}) : combine(Flag<true>{}, Flag<true>{}, Flag<false>{});
-    else p.drag_on ? combine(Flag<true>{}, Flag<false>{}, Flag<true>{}) : combine(Flag<true>{}, Flag<false>{}, Flag<false>{});
-  } else {
-    if (p.has_delta) p.drag_on ? combine(Flag<false>{}, Flag<true>{}, Flag<true>{}) : combine(Flag<false>{}, Flag<true>{}, Flag<false>{});
-    else p.drag_on ? combine(Flag<false>{}, Flag<false>{}, Flag<true>{}) : combine(Flag<false>{}, Flag<false>{}, Flag<false>{});
-  }
+  auto with_cfl = [&](auto b, auto d, auto g) {
+    if (p.want_cfl) combine(b, d, g, Flag<true>{});
+    else combine(b, d, g, Flag<false>{});
+  };
+  auto with_drag = [&](auto b, auto d) {
+    if (p.drag_on) with_cfl(b, d, Flag<true>{});
+    else with_cfl(b, d, Flag<false>{});
+  };
+  auto with_delta = [&](auto b) {
+    if (p.has_delta) with_drag(b, Flag<true>{});
+    else with_drag(b, Flag<false>{});
+  };
+  if (p.blend) with_delta(Flag<true>{});
+  else with_delta(Flag<false>{});
   if (p.want_cfl) {
     double vmax[2] = {static_cast<double>(vmax0), static_cast<double>(vmax1)};
     block_nan_max<2>(vmax, red);
