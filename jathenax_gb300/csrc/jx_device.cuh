@@ -449,21 +449,22 @@ __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, con
   const R lm = u - g.cs, lp = u + g.cs;
   const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
   // Wave strengths am = jd (1/2 + u/(2cs)) - jm/(2cs), az = jq - jd t,
-  // ap = jd (1/2 - u/(2cs)) + jm/(2cs);
+  // ap = jd (1/2 - u/(2cs)) + jm/(2cs) (fluxes.py:150-153);
   // g = (l + r)/2 - (|lm| am e_m + |u| az e_z + |lp| ap e_p)/2 with the
   // eigenvectors e_m = (1, lm, t), e_z = (0, 0, 1), e_p = (1, lp, t).
-  // In float64 am, ap and |u| az are formed halved (every input scaled by
-  // 1/2, so the halves are exact) and each component is one FMA: bit for bit
-  // the halved difference, two float64 operations fewer per face. Float32
-  // keeps the unhalved form, which measured faster in the marching kernel.
+  // In float64 am, ap and |u| az are formed halved and each component of g
+  // is one FMA (two float64 operations fewer per face). Float32 keeps the
+  // direct form, which measured faster in the marching kernel.
   const R s0 = l0 + r0, s1 = l1 + r1, s2 = l2 + r2;
   const R az = fma(jd, -t, jq);
   R g0, g1, g2, dstar, dstar2;
   if constexpr (sizeof(R) == 8) {
-    const R hq = u * g.quarter_inv_cs;  // (u / 4) / cs
-    const R jmq = jm * g.quarter_inv_cs;
-    const R am = fma(jd, R(0.25) + hq, -jmq);  // am / 2
-    const R ap = fma(jd, R(0.25) - hq, jmq);   // ap / 2
+    // am = jd/2 + X/(2cs), ap = jd/2 - X/(2cs) with X = u jd - jm: one FMA
+    // for X serves both (two float64 operations fewer per face).
+    const R X = fma(u, jd, -jm);
+    const R jq4 = R(0.25) * jd;
+    const R am = fma(X, g.quarter_inv_cs, jq4);   // am / 2
+    const R ap = fma(-X, g.quarter_inv_cs, jq4);  // ap / 2
     const R wm = fabs(lm) * am, wz = (R(0.5) * fabs(u)) * az, wp = fabs(lp) * ap;  // halves
     const R wmp = wm + wp;
     g0 = fma(R(0.5), s0, -wmp);
