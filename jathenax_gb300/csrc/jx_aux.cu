@@ -1038,7 +1038,7 @@ __global__ void math_probe_kernel(int64_t n, const R* a, const R* b, R* rcp_out,
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   rcp_out[k] = Num<R>::rcp(b[k]);
-  div_out[k] = Num<R>::div(a[k], b[k]);
+  div_out[k] = Num<R>::quick_div(a[k], b[k]);
   geo_out[k] = Num<R>::geo_mean(fabs(a[k]), fabs(b[k]));
 }
 

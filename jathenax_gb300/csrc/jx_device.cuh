@@ -25,7 +25,8 @@
 // reciprocals of the recovery, the Riemann solvers and the CFL speeds, and
 // the square root of the Roe/HLLE average, are third-order refinements of
 // the unit's float64 seeds (within an ulp; the tolerance against the
-// reference is 1e-12 per stage), and quotients stay correctly rounded.
+// reference is 1e-12 per stage); the PLM, PPMX and HLLE quotients multiply by
+// such a reciprocal, and the WENO-Z quotients stay correctly rounded.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -92,6 +93,7 @@ template <> struct Num<float> {
     if (eb == 0 || eb == 0xff || ea == 0xff) return a / b;
     return a * rcp(b);
   }
+  static __device__ __forceinline__ float quick_div(float a, float b) { return div(a, b); }
   // sqrt(a) sqrt(b) for a, b >= 0
   static __device__ __forceinline__ float geo_mean(float a, float b) { return root(a) * root(b); }
 };
@@ -185,9 +187,17 @@ template <> struct Num<double> {
     const double e = fma(-t, y, 1.0);
     return fma(t, e * fma(e, 0.375, 0.5), t);
   }
-  // a/b correctly rounded. (The reconstruction weights that divide are
-  // kept exact in float64; see the note above.)
+  // a/b correctly rounded (WENO-Z weights; see quick_div).
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  // a/b as a times the refined reciprocal of b (within about 1.5 ulp), the
+  // product rounded on its own (__dmul_rn) so that no kernel can fuse it into
+  // a neighbouring add. Used by PLM, PPMX and HLLE; WENO-Z keeps div, where
+  // this quotient made the batched and single-solve kernels differ in the
+  // last bit.
+  static __device__ __forceinline__ double quick_div(double a, double b) {
+    if (outside_seed_range(b)) return a / b;
+    return __dmul_rn(a, rcp(b));
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -281,7 +291,7 @@ __device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face
   const R scale = N::pmax(fabs(m1), N::pmax(fabs(c), fabs(p1)));
   const bool use = agree && N::pgt(fabs(d2), R(1e-12) * scale);
   R ratio = R(0);
-  if (use) ratio = N::div(lim, d2);
+  if (use) ratio = N::quick_div(lim, d2);
   const bool steep_lo = N::abs_ge_twice(dl, dh), steep_hi = N::abs_ge_twice(dh, dl);
   R lm, hm;
   if constexpr (sizeof(R) == 8) {
@@ -305,7 +315,7 @@ __device__ __forceinline__ void plm_cell(R m1, R c, R p1, R& lo, R& hi) {
   const R bw = c - m1;
   const R fw = p1 - c;
   R hs = R(0);
-  if (N::prod_gt0(bw, fw)) hs = N::div(bw * fw, bw + fw);
+  if (N::prod_gt0(bw, fw)) hs = N::quick_div(bw * fw, bw + fw);
   hi = c + hs;
   lo = c - hs;
 }
@@ -429,7 +439,7 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
   const R vl = ul - bm, vr = ur - bp;
   const R fl0 = dl * vl, fl1 = dl * ul * vl + g.cs2 * dl, fl2 = dl * tl * vl;
   const R fr0 = dr * vr, fr1 = dr * ur * vr + g.cs2 * dr, fr2 = dr * tr * vr;
-  const R w = N::div(R(0.5) * (bp + bm), bp - bm);
+  const R w = N::quick_div(R(0.5) * (bp + bm), bp - bm);
   f0 = R(0.5) * (fl0 + fr0) + w * (fl0 - fr0);
   f1 = R(0.5) * (fl1 + fr1) + w * (fl1 - fr1);
   f2 = R(0.5) * (fl2 + fr2) + w * (fl2 - fr2);
