@@ -277,7 +277,7 @@ jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sin
                        jx_stream s);
 
 /* Arithmetic probe for tests: for i < n, rcp_out[i] = 1/b[i],
- * div_out[i] = a[i]/b[i] (the quotient of the PLM, PPMX and HLLE weights)
+ * div_out[i] = a[i]/b[i] (the quotient of the limiter and HLLE weights)
  * and geo_out[i] = sqrt(|a[i]|) sqrt(|b[i]|) as the stage kernels compute
  * them in `dtype` (device arrays of that type). */
 jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, void* rcp_out,

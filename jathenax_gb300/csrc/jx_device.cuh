@@ -25,8 +25,8 @@
 // reciprocals of the recovery, the Riemann solvers and the CFL speeds, and
 // the square root of the Roe/HLLE average, are third-order refinements of
 // the unit's float64 seeds (within an ulp; the tolerance against the
-// reference is 1e-12 per stage); the PLM, PPMX and HLLE quotients multiply by
-// such a reciprocal, and the WENO-Z quotients stay correctly rounded.
+// reference is 1e-12 per stage), and the PLM, PPMX, WENO-Z and HLLE
+// quotients multiply by such a reciprocal.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -187,13 +187,11 @@ template <> struct Num<double> {
     const double e = fma(-t, y, 1.0);
     return fma(t, e * fma(e, 0.375, 0.5), t);
   }
-  // a/b correctly rounded (WENO-Z weights; see quick_div).
+  // a/b correctly rounded.
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
   // a/b as a times the refined reciprocal of b (within about 1.5 ulp), the
   // product rounded on its own (__dmul_rn) so that no kernel can fuse it into
-  // a neighbouring add. Used by PLM, PPMX and HLLE; WENO-Z keeps div, where
-  // this quotient made the batched and single-solve kernels differ in the
-  // last bit.
+  // a neighbouring add. Used by the PLM, PPMX, WENO-Z and HLLE weights.
   static __device__ __forceinline__ double quick_div(double a, double b) {
     if (outside_seed_range(b)) return a / b;
     return __dmul_rn(a, rcp(b));
@@ -320,6 +318,49 @@ __device__ __forceinline__ void plm_cell(R m1, R c, R p1, R& lo, R& hi) {
   lo = c - hs;
 }
 
+// Float64 WENO-Z with every rounding spelled out (explicit FMAs and
+// unfusable _rn operations): the compiler has no contraction left to choose,
+// so every kernel instantiation forms the same bits, and the quotients can
+// use the refined reciprocal (quick_div) without the batched and
+// single-solve kernels drifting apart in the last bit.
+__device__ __forceinline__ double wenoz_combine_f64(double s0, double s1, double s2, double s3, double s4,
+                                                     double w0, double w1, double w2) {
+  // fluxes.py:87-93.
+  const double a0 = __dmul_rn(0.1, w0), a1 = __dmul_rn(0.6, w1), a2 = __dmul_rn(0.3, w2);
+  const double f0 = fma(11.0, s2, fma(-7.0, s1, __dmul_rn(2.0, s0)));
+  const double f1 = fma(2.0, s3, fma(5.0, s2, -s1));
+  const double f2 = __dsub_rn(fma(5.0, s3, __dmul_rn(2.0, s2)), s4);
+  const double num = fma(f2, a2, fma(f1, a1, __dmul_rn(f0, a0)));
+  const double den = __dmul_rn(6.0, __dadd_rn(__dadd_rn(a0, a1), a2));
+  return Num<double>::quick_div(num, den);
+}
+
+__device__ __forceinline__ void wenoz_cell_f64(double m2, double m1, double c, double p1, double p2, double& lo,
+                                               double& hi) {
+  // fluxes.py:96-117; eps = max(1e-42, finfo(float64).tiny) at fluxes.py:108.
+  using N = Num<double>;
+  const double k1312 = 13.0 / 12.0, eps = 1e-42;
+  const double t0 = fma(-2.0, m1, __dadd_rn(m2, c)), u0 = fma(-4.0, m1, fma(3.0, c, m2));
+  const double t1 = fma(-2.0, c, __dadd_rn(m1, p1)), u1 = __dsub_rn(m1, p1);
+  const double t2 = fma(-2.0, p1, __dadd_rn(p2, c)), u2 = fma(-4.0, p1, fma(3.0, c, p2));
+  const double b0 = fma(k1312, __dmul_rn(t0, t0), __dmul_rn(0.25, __dmul_rn(u0, u0)));
+  const double b1 = fma(k1312, __dmul_rn(t1, t1), __dmul_rn(0.25, __dmul_rn(u1, u1)));
+  const double b2 = fma(k1312, __dmul_rn(t2, t2), __dmul_rn(0.25, __dmul_rn(u2, u2)));
+  const double tau = fabs(__dsub_rn(b0, b2));
+  const double d0 = __dadd_rn(b0, eps), d1 = __dadd_rn(b1, eps), d2 = __dadd_rn(b2, eps);
+  const double dmin = N::pmin(d0, N::pmin(d1, d2));
+  const double inv_sc = N::quick_div(1.0, N::pmax(tau, dmin));
+  double base = __dmul_rn(dmin, inv_sc);
+  base = __dmul_rn(base, base);
+  const double con = __dmul_rn(tau, inv_sc);
+  const double r0 = __dmul_rn(con, N::quick_div(dmin, d0));
+  const double r1 = __dmul_rn(con, N::quick_div(dmin, d1));
+  const double r2 = __dmul_rn(con, N::quick_div(dmin, d2));
+  const double w0 = fma(r0, r0, base), w1 = fma(r1, r1, base), w2 = fma(r2, r2, base);
+  hi = wenoz_combine_f64(m2, m1, c, p1, p2, w0, w1, w2);
+  lo = wenoz_combine_f64(p2, p1, c, m1, m2, w2, w1, w0);
+}
+
 template <typename R>
 __device__ __forceinline__ R wenoz_combine(R s0, R s1, R s2, R s3, R s4, R w0, R w1, R w2) {
   // fluxes.py:87-93.
@@ -332,6 +373,10 @@ __device__ __forceinline__ R wenoz_combine(R s0, R s1, R s2, R s3, R s4, R w0, R
 
 template <typename R>
 __device__ __forceinline__ void wenoz_cell(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
+  if constexpr (sizeof(R) == 8) {
+    wenoz_cell_f64(m2, m1, c, p1, p2, lo, hi);
+    return;
+  }
   // fluxes.py:96-117; eps = max(1e-42, finfo(dtype).tiny) at fluxes.py:108.
   using N = Num<R>;
   const R k1312 = R(13.0 / 12.0);

@@ -4,7 +4,7 @@
 The float64 reciprocal and square root are third-order refinements of the
 special-function unit's seeds and must stay within 1 ulp of the correctly
 rounded results over the whole seeded range, with IEEE results (inf, NaN,
-subnormal handling) outside it; the float64 quotient of the PLM/PPMX/HLLE
+subnormal handling) outside it; the float64 quotient of the limiter/HLLE
 weights multiplies by that reciprocal and must stay within 2 ulp (IEEE
 outside the range); float32 uses the unit's approximations and must stay
 within 2-3 ulp.
