@@ -179,25 +179,43 @@ def nvidia_smi_index(local_rank):
 # ---------------------------------------------------------------------------
 # Our arm.
 # ---------------------------------------------------------------------------
-def fma_peak_tflops(torch, _lib, dtype_id):
-    """Measured FMA throughput (TFLOP/s) of the FP64 or FP32 pipe, all SMs busy."""
+def fma_peak(torch, _lib, dtype_id, gpu_index=None):
+    """Measured FMA throughput of the FP64 or FP32 pipe with every SM busy.
+
+    Sweeps 8/16/32 independent chains per thread at 4 and 8 resident blocks
+    of 256 threads per SM and keeps the fastest; with ``gpu_index`` the SM
+    clock is sampled meanwhile, so the rate is also stated as FMAs per SM
+    per clock cycle. Returns {"tflops", "fma_per_sm_per_clk", "sm_mhz",
+    "sms", "trials"}.
+    """
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, iters = sms * 8, 4096 if dtype_id == _lib.JX_F64 else 65536
-    sink = torch.zeros(blocks, dtype=torch.float64, device="cuda")
+    sink = torch.zeros(sms * 8, dtype=torch.float64, device="cuda")
     stream = _lib.stream_handle()
-    for _ in range(2):
-        _lib.call("jx_probe_fma", dtype_id, blocks, iters, _lib.ptr(sink), stream)
+    rate = 1.2e12 if dtype_id == _lib.JX_F64 else 90e12  # flop/s, to size ~25 ms launches
+    sampler = ClockSampler(gpu_index) if gpu_index is not None else None
+    trials = []
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = None
-    for _ in range(3):
-        start.record()
-        _lib.call("jx_probe_fma", dtype_id, blocks, iters, _lib.ptr(sink), stream)
-        end.record()
-        end.synchronize()
-        ms = start.elapsed_time(end)
-        best = ms if best is None else min(best, ms)
-    flops = 2.0 * 8 * iters * blocks * 256
-    return flops / (best * 1e-3) / 1e12
+    for chains in (8, 16, 32):
+        for per_sm in (4, 8):
+            blocks = sms * per_sm
+            iters = max(64, int(0.025 * rate / (2.0 * chains * blocks * 256)))
+            _lib.call("jx_probe_fma", dtype_id, blocks, iters, chains, _lib.ptr(sink), stream)
+            best = None
+            for _ in range(3):
+                start.record()
+                _lib.call("jx_probe_fma", dtype_id, blocks, iters, chains, _lib.ptr(sink), stream)
+                end.record()
+                end.synchronize()
+                ms = start.elapsed_time(end)
+                best = ms if best is None else min(best, ms)
+            flops = 2.0 * chains * iters * blocks * 256
+            trials.append({"chains": chains, "blocks_per_sm": per_sm, "tflops": round(flops / (best * 1e-3) / 1e12, 4)})
+    clocks = sampler.stop() if sampler is not None else {"sm_mhz": None}
+    top = max(trials, key=lambda r: r["tflops"])
+    mhz = clocks.get("sm_mhz")
+    per_clk = top["tflops"] * 1e12 / 2.0 / (sms * mhz * 1e6) if mhz else None
+    return {"tflops": top["tflops"], "fma_per_sm_per_clk": None if per_clk is None else round(per_clk, 3),
+            "sm_mhz": mhz, "sms": sms, "best": {k: top[k] for k in ("chains", "blocks_per_sm")}, "trials": trials}
 
 
 def measured_peaks():
@@ -322,13 +340,13 @@ def bench_ours(args, world, rank, local):
     n = args.n
     U0 = torch.as_tensor(kelvin_helmholtz_tanh(n, n), device="cuda")
     peaks, peak_kind = measured_peaks()
-    fp64_peak = fma_peak_tflops(torch, _lib, _lib.JX_F64)
-    fp32_peak = fma_peak_tflops(torch, _lib, _lib.JX_F32)
-
     if args.only_fp32:
         r32 = run_precision(torch, _lib, Solve, U0, n, torch.float32, args, world)
         return {"metric": METRIC, "value": round(r32["value"], 1), "unit": METRIC, "dtype": "f32",
                 "ms_per_step": round(r32["ms"] / args.steps, 4), "stage_ms": r32["stage_ms"]}
+    gpu = nvidia_smi_index(local)
+    probe64 = fma_peak(torch, _lib, _lib.JX_F64, gpu)
+    probe32 = fma_peak(torch, _lib, _lib.JX_F32, gpu)
     r64 = run_precision(torch, _lib, Solve, U0, n, torch.float64, args, world,
                         clocks=nvidia_smi_index(local))
     r32 = None if args.no_fp32 else run_precision(torch, _lib, Solve, U0, n, torch.float32, args, world)
@@ -337,7 +355,8 @@ def bench_ours(args, world, rank, local):
     fpcs = flops_per_cell_stage("ppm4/roe/nvar4")
     nvar, w64 = 4, 8
 
-    def roofline(res, w, peak_tflops, key):
+    def roofline(res, w, probe, key):
+        peak_tflops = probe["tflops"]
         flops = cells * fpcs / (res["stage_ms"] * 1e-3) / 1e12
         stage_bytes = 3 * w * nvar * cells  # stage >= 2: read U and V, write U
         gbs = stage_bytes / (res["stage_ms"] * 1e-3) / 1e9
@@ -358,6 +377,15 @@ def bench_ours(args, world, rank, local):
                "hbm": {"achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                        "frac": round(hbm_frac, 4), "peak_source": f"hbm_gbs of {peak_kind}",
                        "bytes_per_launch": stage_bytes}}
+        out["probe"] = {k: probe[k] for k in ("fma_per_sm_per_clk", "sm_mhz", "sms", "best")}
+        if key == "f64":
+            # The same work against GB300's nominal float64 rate, 2 DFMA per SM
+            # per clock at the SM clock sampled during the timed steps.
+            mhz = (res.get("clocks") or {}).get("sm_mhz") or probe["sm_mhz"]
+            if mhz:
+                nominal = 2 * 2 * probe["sms"] * mhz * 1e6 / 1e12
+                out["fp64_nominal"] = {"peak": round(nominal, 4), "unit": "TFLOP/s", "frac": round(flops / nominal, 4),
+                                       "peak_source": f"2 DFMA/SM/clk x {probe['sms']} SMs x {mhz:.0f} MHz"}
         if bound == "hbm":
             out.update(achieved=round(gbs, 1), peak=hbm_peak, unit="GB/s", frac=round(hbm_frac, 4),
                        peak_source=f"hbm_gbs of {peak_kind}")
@@ -373,7 +401,7 @@ def bench_ours(args, world, rank, local):
                    "step": "one evolve cycle: CFL dt + 3 fused RK stages (CUDA graph replay)",
                    "l2": f"state {cells * 4 * 8 / 1e6:.0f} MB > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},
-        "roofline": roofline(r64, w64, fp64_peak, "f64"),
+        "roofline": roofline(r64, w64, probe64, "f64"),
         "e2e": r64["e2e"],
         "gpu_launches": 4 * args.steps,  # per step: begin-step + 3 stage kernels
         "clocks": r64["clocks"],
@@ -381,7 +409,7 @@ def bench_ours(args, world, rank, local):
     if r32 is not None:
         line["fp32"] = {"value": round(r32["value"], 1), "unit": METRIC,
                         "ms_per_step": round(r32["ms"] / args.steps, 4), "dtype": "f32",
-                        "roofline": roofline(r32, 4, fp32_peak, "f32"), "e2e": r32["e2e"],
+                        "roofline": roofline(r32, 4, probe32, "f32"), "e2e": r32["e2e"],
                         "gpu_launches": 4 * args.steps}
     if rank == 0 and world == 1 and args.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
@@ -389,7 +417,36 @@ def bench_ours(args, world, rank, local):
         line["batched"] = bench_batched(torch)
         line["serving"] = bench_serving(torch, args.serve_requests)
         line["precision"] = bench_precision(torch)
+    line["summary"] = summary(line)  # last key: the end of the printed line
     return line
+
+
+def summary(line):
+    """The headline numbers of every block, compact, for the end of the JSON line."""
+    out = {"f64": {"cell_updates_per_s": line["value"], "e2e": round(line["e2e"]["value"], 1),
+                   "stage_ms": line["roofline"]["stage_ms"], "frac_of_probe": line["roofline"]["frac"],
+                   "frac_of_nominal": (line["roofline"].get("fp64_nominal") or {}).get("frac")}}
+    if "fp32" in line:
+        r = line["fp32"]["roofline"]
+        out["f32"] = {"cell_updates_per_s": line["fp32"]["value"], "e2e": round(line["fp32"]["e2e"]["value"], 1),
+                      "stage_ms": r["stage_ms"], "hbm_frac": r["hbm"]["frac"]}
+    b = line.get("batched")
+    if b:
+        out["batched"] = {k: b[k] for k in ("speedup", "batched_fp32_solves_per_s", "serial_fp64_solves_per_s",
+                                             "max_l1_density_err_fp32_vs_fp64", "min_cycles_1024", "tile")}
+    sv = line.get("serving")
+    if sv:
+        out["serving"] = {k: [v["solves_per_s"], v["speedup_vs_serial_fp64"], v["tts_p50_s"], v["tts_p99_s"],
+                              v["arrival_bound"]]
+                          for k, v in sv.items() if isinstance(v, dict) and "solves_per_s" in v}
+        out["serving_fields"] = ["solves_per_s", "speedup_vs_serial_fp64", "p50_s", "p99_s", "arrival_bound"]
+        errs = [v["fp32_l1_density_err_vs_fp64_max"] for v in sv.values()
+                if isinstance(v, dict) and v.get("fp32_l1_density_err_vs_fp64_max") is not None]
+        out["serving_fp32_l1_max"] = max(errs) if errs else None
+    p = line.get("precision")
+    if p:
+        out["precision_l1_density"] = {k: v["l1_density"] for k, v in p.items()}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -415,7 +472,7 @@ def make_request(kind, side, seed, tlim, dtype, rid=0):
                    tlim=tlim, dtype=dtype, seed=seed or 1)
 
 
-def bench_batched(torch, tlim=0.02):
+def bench_batched(torch, tlim=0.05):
     """Batched ensemble (float32, one persistent launch per stage, graph-captured)
     against looping the plain float64 kernel over the same 64 solves."""
     from jathenax_gb300 import autotune
@@ -433,6 +490,7 @@ def bench_batched(torch, tlim=0.02):
     torch.cuda.synchronize()
     batched_s = time.perf_counter() - t0
     out32 = [s.S.cpu().numpy() for s in solves]
+    cycles = [c.cycle for c in bank.read()]
     del batch, solves
     t0 = time.perf_counter()
     l1 = []
@@ -449,6 +507,8 @@ def bench_batched(torch, tlim=0.02):
             "serial_fp64_solves_per_s": round(len(reqs) / serial_s, 3),
             "speedup": round(serial_s / batched_s, 2),
             "max_l1_density_err_fp32_vs_fp64": max(l1),
+            "min_cycles_1024": min(c for c, r in zip(cycles, reqs) if r.side == 1024),
+            "cycles_range": [min(cycles), max(cycles)],
             "tile": tuned["tile"], "blocks_per_sm": tuned["blocks_per_sm"],
             "autotune_ms_per_step": {f"{t['tile'][0]}x{t['tile'][1]}": round(t["ms_per_step"], 3)
                                      for t in tuned["trials"]},

@@ -125,8 +125,10 @@ jx_status jx_timestep(const jx_desc* d, const void* W, double cfl, double prev_d
  * enough for every grid jx_check_desc accepts; a grid that needed more would
  * be refused with JX_ERR_INVALID). The first call on a device looks up the
  * array's address on that device; make that first call before any stream
- * capture. Calls share the array: calls whose kernels overlap on the GPU
- * race. Allocates nothing. */
+ * capture. The address is kept per device for the life of the process: after
+ * cudaDeviceReset (which unloads the library's device code) it is stale, so
+ * do not call this entry point on a device that has been reset. Calls share
+ * the array: calls whose kernels overlap on the GPU race. Allocates nothing. */
 jx_status jx_timestep_noalloc(const jx_desc* d, const void* W, double cfl, double prev_dt,
                               double time, double tlim, double* dt_out, jx_stream s);
 
@@ -269,11 +271,12 @@ int32_t jx_ou_table(const int32_t* modes, int32_t n_modes, double Lx, double Ly,
                     int32_t nhigh, double npeak, double sol_fraction, int64_t seed, double tcorr,
                     double dt_update, int32_t updates, double* out);
 
-/* Peak probe: `blocks` x 256 threads each run 8 independent chains of
- * `iters` dependent FMAs in the given dtype (2*8*iters flops per thread).
- * Timed by the caller with events to measure the FP64/FP32 pipe rate.
- * sink (device, >= blocks doubles) is never written in practice. */
-jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sink,
+/* Peak probe: `blocks` x 256 threads each run `chains` (8, 16 or 32)
+ * independent chains of `iters` dependent FMAs in the given dtype
+ * (2*chains*iters flops per thread). Timed by the caller with events to
+ * measure the FP64/FP32 pipe rate. sink (device, >= blocks doubles) is never
+ * written in practice. No counterpart in the reference. */
+jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, int32_t chains, double* sink,
                        jx_stream s);
 
 /* Arithmetic probe for tests: for i < n, rcp_out[i] = 1/b[i],

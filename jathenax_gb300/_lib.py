@@ -96,7 +96,7 @@ PROTOTYPES = {
     "jx_face_velocity_gradients": [_I32, _I32, _I32, _I32, _P, _D, _D, _I32, _P, _P, _P],
     "jx_smagorinsky_viscosity": [_I32, _I64, _P, _P, _D, _D, _D, _P, _P],
     "jx_tile_info": [_DP, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
-    "jx_probe_fma": [_I32, _I32, _I32, _P, _P],
+    "jx_probe_fma": [_I32, _I32, _I32, _I32, _P, _P],
     "jx_probe_math": [_I32, _I64, _P, _P, _P, _P, _P, _P],
     "jx_batch_plan_bytes": [ctypes.POINTER(SolveStruct), _I32, ctypes.POINTER(_SZ)],
     "jx_batch_plan": [ctypes.POINTER(SolveStruct), _I32, _P, _SZ],

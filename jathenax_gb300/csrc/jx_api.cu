@@ -84,11 +84,12 @@ struct Tile {
   size_t smem;       // generic kernel
   bool fast_shape;   // 3/4 variables at tile width 32: the fast kernel applies
   size_t fast_smem;  // fast kernel
-  // Register-marching kernel (3/4 variables): kMarchTileX x mty tiles. The
-  // shared-memory tile above stays resolved for stages that fall back
-  // (trace outputs requested, 4-variable arrays not 16-byte aligned).
+  // Register-marching kernel (3/4 variables): march_tile_x(mnc) x mty tiles,
+  // mnc columns per lane. The shared-memory tile above stays resolved for
+  // stages that fall back (trace outputs requested, 4-variable arrays not
+  // 16-byte aligned).
   bool march;
-  int mty, mtiles_x, mtiles_y;
+  int mnc, mty, mtiles_x, mtiles_y;
   size_t cfl_slots;  // CFL partial slots the workspace holds
 };
 
@@ -96,19 +97,19 @@ int sm_count();
 
 // Resident marching blocks per SM for this descriptor on the current device
 // (cached; 4 when the device cannot be queried).
-int march_occupancy(const jx_desc* d) {
-  static int cache[64][2][5][3][2];
+int march_occupancy(const jx_desc* d, int nc) {
+  static int cache[64][2][5][3][2][3];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 4;
-  int& c = cache[dev][d->dtype][d->recon][d->rsolver][d->nvar - 3];
+  int& c = cache[dev][d->dtype][d->recon][d->rsolver][d->nvar - 3][nc - 1];
   if (c == 0) {
     int n = 0;
     switch (d->recon) {
-      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, false); break;
-      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, false); break;
-      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, false); break;
-      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, false); break;
-      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, false); break;
+      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, nc, false); break;
+      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, nc, false); break;
+      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, nc, false); break;
+      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, nc, false); break;
+      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, nc, false); break;
     }
     if (n < 1) {
       cudaGetLastError();
@@ -123,10 +124,10 @@ int march_occupancy(const jx_desc* d) {
 // the resident warp slots of the device, finish soonest. A tile of h rows
 // costs about h + 2.5 row-updates (the 6 leading rows of the walk do the y
 // work only); the grid runs in ceil(tiles / slots) rounds.
-int march_rows(const jx_desc* d) {
+int march_rows(const jx_desc* d, int nc) {
   static const int kRows[] = {8, 12, 16, 24, 32, 48, 64};
-  const int64_t slots = (int64_t)sm_count() * march_occupancy(d) * kMarchWarps;
-  const int64_t cols = (d->nx + kMarchTileX - 1) / kMarchTileX;
+  const int64_t slots = (int64_t)sm_count() * march_occupancy(d, nc) * kMarchWarps;
+  const int64_t cols = (d->nx + march_tile_x(nc) - 1) / march_tile_x(nc);
   int best = kRows[0];
   double best_cost = 1e300;
   for (int h : kRows) {
@@ -142,11 +143,16 @@ int march_rows(const jx_desc* d) {
 }
 
 jx_status resolve_tile(const jx_desc* d, Tile* t, bool device = true) {
-  // Automatic tiles: float32 marches; float64, bound by the FP64 pipe,
-  // keeps the shared-memory tile, which evaluates no halo faces twice.
+  // Automatic tiles: float32 marches with two columns per lane; float64,
+  // bound by the FP64 pipe, keeps the shared-memory tile, which evaluates no
+  // halo faces twice. An explicit tile width of 26, 58 or 90 asks for the
+  // marching kernel with 1, 2 or 3 columns per lane (float64: 58 only).
   const bool three_four = d->nvar == 3 || d->nvar == 4;
-  const bool march = three_four && (d->tile_x == kMarchTileX ||
-                                    (d->tile_x == 0 && d->tile_y == 0 && d->dtype == JX_F32));
+  const int want_nc = march_cols(d->tile_x);
+  const bool march = three_four && (want_nc > 0 || (d->tile_x == 0 && d->tile_y == 0 && d->dtype == JX_F32));
+  const int nc = want_nc > 0 ? want_nc : 2;
+  if (march && d->dtype == JX_F64 && nc != 2)
+    return fail(JX_ERR_INVALID, "float64 marching tiles are %d columns wide, not %d", kMarchTileX, d->tile_x);
   int tx = d->tile_x > 0 && !march ? d->tile_x : 32;
   int ty = d->tile_y > 0 && !march ? d->tile_y : 16;
   size_t smem = stage_smem_bytes(d->recon, d->dtype, d->nvar, tx, ty);
@@ -174,18 +180,19 @@ jx_status resolve_tile(const jx_desc* d, Tile* t, bool device = true) {
   t->smem = smem;
   if ((int64_t)t->tiles_x * t->tiles_y > ((int64_t)1 << 31) - 1) return fail(JX_ERR_INVALID, "too many tiles");
   t->march = march;
-  t->mty = t->mtiles_x = t->mtiles_y = 0;
+  t->mnc = t->mty = t->mtiles_x = t->mtiles_y = 0;
   size_t slots = (size_t)t->tiles_x * t->tiles_y;
   if (march) {
     if (d->tile_y > 0 && d->tile_y < kMarchMinRows)
       return fail(JX_ERR_INVALID, "marching tiles need at least %d rows", kMarchMinRows);
     // The workspace covers the shortest automatic marching tile, so its
     // size does not depend on the device.
-    const int64_t cols = (d->nx + kMarchTileX - 1) / kMarchTileX;
+    const int64_t cols = (d->nx + march_tile_x(nc) - 1) / march_tile_x(nc);
     const int rows_min = d->tile_y > 0 ? d->tile_y : kMarchMinRows;
     const size_t mslots = (size_t)(cols * ((d->ny + rows_min - 1) / rows_min));
     if (mslots > slots) slots = mslots;
-    t->mty = d->tile_y > 0 ? d->tile_y : (device ? march_rows(d) : kMarchMinRows);
+    t->mnc = nc;
+    t->mty = d->tile_y > 0 ? d->tile_y : (device ? march_rows(d, nc) : kMarchMinRows);
     t->mtiles_x = (int)cols;
     t->mtiles_y = (d->ny + t->mty - 1) / t->mty;
   }
@@ -289,7 +296,8 @@ cudaError_t launch_march(int recon, int dtype, int rsolver, const StageParams& p
 cudaError_t launch_stage(const jx_desc* d, const StageParams& p, const Tile& t, cudaStream_t s) {
   if (use_march(d, p, t)) {
     StageParams m = p;
-    m.tx = kMarchTileX;
+    m.tx = march_tile_x(t.mnc);
+    m.nc = t.mnc;
     m.ty = t.mty;
     m.tiles_x = t.mtiles_x;
     return launch_march(d->recon, d->dtype, d->rsolver, m, dim3((unsigned)((int64_t)t.mtiles_x * t.mtiles_y)), s);
@@ -454,7 +462,7 @@ jx_status jx_tile_info(const jx_desc* d, int32_t* tile_x, int32_t* tile_y, int64
   if (st) return st;
   Tile t;
   if ((st = resolve_tile(d, &t))) return st;
-  if (tile_x) *tile_x = t.march ? kMarchTileX : t.tx;
+  if (tile_x) *tile_x = t.march ? march_tile_x(t.mnc) : t.tx;
   if (tile_y) *tile_y = t.march ? t.mty : t.ty;
   if (smem_bytes) *smem_bytes = t.march ? 0 : (int64_t)t.smem;
   return JX_OK;
@@ -675,10 +683,11 @@ jx_status jx_smagorinsky_viscosity(int32_t dtype, int64_t ncell, const void* dv_
   return cuda_check(launch_smagorinsky(dtype, ncell, dv_dx, dv_dy, c, out, (cudaStream_t)s), "Smagorinsky kernel");
 }
 
-jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, double* sink, jx_stream s) {
+jx_status jx_probe_fma(int32_t dtype, int32_t blocks, int32_t iters, int32_t chains, double* sink, jx_stream s) {
   if (dtype != JX_F64 && dtype != JX_F32) return fail(JX_ERR_UNSUPPORTED, "unknown dtype %d", dtype);
-  if (blocks < 1 || iters < 1 || !sink) return fail(JX_ERR_INVALID, "bad probe arguments");
-  return cuda_check(launch_probe(dtype, blocks, iters, sink, (cudaStream_t)s), "probe kernel");
+  if (blocks < 1 || iters < 1 || !sink || (chains != 8 && chains != 16 && chains != 32))
+    return fail(JX_ERR_INVALID, "bad probe arguments");
+  return cuda_check(launch_probe(dtype, blocks, iters, chains, sink, (cudaStream_t)s), "probe kernel");
 }
 
 jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, void* rcp_out, void* div_out,
@@ -699,11 +708,14 @@ jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, 
 namespace {
 
 constexpr uint32_t kPlanMagic = 0x4a584250;  // "JXBP"
-constexpr int kMaxGroups = 90;  // 2 precisions x 5 reconstructions x 3 solvers x 3 kernel/count classes
+// 2 precisions x 5 reconstructions x 3 solvers x 7 kernel classes (shared
+// memory; marching with 3 or 4 variables at 1, 2 or 3 columns per lane)
+constexpr int kMaxGroups = 210;
 
 struct BatchGroup {
   int dtype, recon, rsolver, first, count, tile_first, nwork, march;
   int nv;   // marching groups: the variable count of every solve (0 in shared-memory groups)
+  int nc;   // marching groups: columns per lane (0 in shared-memory groups)
   int bps;  // resident blocks per SM of the group's kernel (occupancy at plan time)
   size_t smem;
 };
@@ -790,24 +802,24 @@ cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* p
   }
 }
 
-int batch_march_occupancy(int recon, int dtype, int rsolver, int nv) {
+int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc) {
   switch (recon) {
-    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, true);
-    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, true);
-    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, true);
-    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, true);
-    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, true);
+    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, true);
+    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, true);
+    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, true);
+    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, true);
+    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, true);
   }
 }
 
-cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, const StageParams* params,
+cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, int nc, const StageParams* params,
                                const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   switch (recon) {
-    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
-    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
-    default: return launch_batch_march_wenoz(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    default: return launch_batch_march_wenoz(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
   }
 }
 
@@ -854,8 +866,7 @@ jx_status check_batch_solve(int i, const jx_solve& in, Tile* t, Ws* w) {
     return fail(JX_ERR_INVALID, "solve %d: 4-variable states must be 16-byte aligned", i);
   if ((st = resolve_tile(&d, t))) return fail(st, "solve %d: %s", i, jx_last_error());
   if (!t->march && !t->fast_shape)
-    return fail(JX_ERR_INVALID, "solve %d: batch tiles are 32 x h or %d x h, not %d x %d", i, kMarchTileX, t->tx,
-                t->ty);
+    return fail(JX_ERR_INVALID, "solve %d: batch tiles are 32 x h or 26/58/90 x h, not %d x %d", i, t->tx, t->ty);
   if (!t->march && t->ty > 64) return fail(JX_ERR_INVALID, "solve %d: batch tiles have at most 64 rows", i);
   if ((st = bind_ws(&d, *t, in.workspace, in.workspace_bytes, w))) return fail(st, "solve %d: %s", i, jx_last_error());
   if (in.forcing.raw_force && (!in.forcing.table || !in.forcing.cos_x || !in.forcing.sin_x || !in.forcing.cos_y ||
@@ -914,10 +925,11 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
     const jx_desc& d = sv[i].desc;
     const int march = tl[i].march ? 1 : 0;
     const int nv = march ? d.nvar : 0;
+    const int nc = march ? tl[i].mnc : 0;
     int g = 0;
     while (g < n_groups && !(h->groups[g].dtype == d.dtype && h->groups[g].recon == d.recon &&
                              h->groups[g].rsolver == d.rsolver && h->groups[g].march == march &&
-                             h->groups[g].nv == nv))
+                             h->groups[g].nv == nv && h->groups[g].nc == nc))
       ++g;
     if (g == n_groups) {
       if (n_groups == kMaxGroups) return fail(JX_ERR_INVALID, "more than %d solver groups", kMaxGroups);
@@ -927,6 +939,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
       G.rsolver = d.rsolver;
       G.march = march;
       G.nv = nv;
+      G.nc = nc;
       G.smem = 0;
     }
     if (!march && tl[i].fast_smem > h->groups[g].smem) h->groups[g].smem = tl[i].fast_smem;
@@ -973,7 +986,8 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
         P = make_stage_params(&d, t, w, stage, in, sv[i].S, out, stage == nst ? nullptr : sv[i].S, nullptr,
                               forced, sv[i].clock, nullptr);
         if (G.march) {
-          P.tx = kMarchTileX;
+          P.tx = march_tile_x(t.mnc);
+          P.nc = t.mnc;
           P.ty = t.mty;
           P.tiles_x = t.mtiles_x;
         }
@@ -987,7 +1001,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
   h->n_groups = n_groups;
   for (int g = 0; g < n_groups; ++g) {
     BatchGroup& G = h->groups[g];
-    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv)
+    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv, G.nc)
                     : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
     if (G.bps < 1) {
       cudaGetLastError();  // no device to query: one block per SM
@@ -1090,7 +1104,7 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
       const int* offs = offsets_dev + G.tile_first;
       cudaStream_t gs = side ? side->s[g % kSideStreams] : s;
       const cudaError_t e =
-          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, P, offs, G.count, G.nwork,
+          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, G.nc, P, offs, G.count, G.nwork,
                                        dim3((unsigned)blocks), gs)
                   : launch_batch(G.recon, G.dtype, G.rsolver, P, offs, G.count, G.nwork, dim3((unsigned)blocks),
                                  G.smem, gs);
@@ -1148,6 +1162,8 @@ namespace {
 
 constexpr size_t kNoAllocSlots = jx::kCflBlocksMax;
 constexpr size_t kNoAllocBytes = jx::kWsHeader + kNoAllocSlots * jx::kCflSlots * sizeof(double);
+// cfl_grid() never launches more than kCflBlocksMax blocks, so every grid fits.
+static_assert(kNoAllocSlots >= (size_t)jx::kCflBlocksMax, "timestep scratch must hold every CFL partial");
 static __device__ __align__(256) unsigned char g_timestep_scratch[kNoAllocBytes];
 
 std::mutex g_scratch_mutex;
@@ -1179,8 +1195,14 @@ extern "C" jx_status jx_timestep_noalloc(const jx_desc* d, const void* W, double
   jx_status st = check_desc(d);
   if (st) return st;
   if (!W || !dt_out) return fail(JX_ERR_INVALID, "null W or dt_out");
+  // The same descriptors as jx_timestep: an explicit tile it would refuse
+  // (too much shared memory, too few marching rows) is refused here too.
+  Tile t;
+  if ((st = resolve_tile(d, &t, false))) return st;
   const int64_t ncell = (int64_t)d->ny * d->nx;
   const size_t need = kWsHeader + (size_t)cfl_grid(ncell) * kCflSlots * sizeof(double);
+  // Unreachable while cfl_grid caps its blocks (static_assert above); kept so
+  // that a change to that cap fails loudly instead of overrunning the array.
   if (need > kNoAllocBytes)
     return fail(JX_ERR_INVALID, "grid of %lld cells needs %zu bytes of timestep scratch; the static scratch holds %zu",
                 (long long)ncell, need, kNoAllocBytes);

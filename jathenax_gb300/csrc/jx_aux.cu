@@ -860,19 +860,31 @@ __global__ void box_sum_finish_kernel(const double* part, int nblk, int nv, doub
   }
 }
 
-// FMA throughput probe: 8 independent dependent-FMA chains per thread.
-template <typename T>
+// FMA throughput probe: C independent dependent-FMA chains per thread, the
+// loop unrolled four times so that loop control is a small share of issue.
+template <typename T, int C>
 __global__ void fma_probe_kernel(int iters, double* sink) {
-  T a[8];
+  T a[C];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) a[c] = T(threadIdx.x + c) * T(1e-3);
+  for (int c = 0; c < C; ++c) a[c] = T(threadIdx.x + c) * T(1e-3);
   const T b = T(0.9999999), d = T(1e-7);
+#pragma unroll 4
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
-    for (int c = 0; c < 8; ++c) a[c] = fma(a[c], b, d);
+    for (int c = 0; c < C; ++c) a[c] = fma(a[c], b, d);
   }
-  T s = a[0] + a[1] + a[2] + a[3] + a[4] + a[5] + a[6] + a[7];
+  T s = T(0);
+#pragma unroll
+  for (int c = 0; c < C; ++c) s += a[c];
   if (s == T(-12345.0)) sink[blockIdx.x] = static_cast<double>(s);  // never true; keeps the chains live
+}
+
+template <typename T>
+cudaError_t launch_probe_typed(int blocks, int iters, int chains, double* sink, cudaStream_t s) {
+  if (chains == 8) fma_probe_kernel<T, 8><<<blocks, 256, 0, s>>>(iters, sink);
+  else if (chains == 16) fma_probe_kernel<T, 16><<<blocks, 256, 0, s>>>(iters, sink);
+  else fma_probe_kernel<T, 32><<<blocks, 256, 0, s>>>(iters, sink);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -1055,10 +1067,9 @@ cudaError_t launch_math_probe(int dtype, int64_t n, const void* a, const void* b
   return cudaGetLastError();
 }
 
-cudaError_t launch_probe(int dtype, int blocks, int iters, double* sink, cudaStream_t s) {
-  if (dtype == JX_F64) fma_probe_kernel<double><<<blocks, 256, 0, s>>>(iters, sink);
-  else fma_probe_kernel<float><<<blocks, 256, 0, s>>>(iters, sink);
-  return cudaGetLastError();
+cudaError_t launch_probe(int dtype, int blocks, int iters, int chains, double* sink, cudaStream_t s) {
+  return dtype == JX_F64 ? launch_probe_typed<double>(blocks, iters, chains, sink, s)
+                         : launch_probe_typed<float>(blocks, iters, chains, sink, s);
 }
 
 }  // namespace jx

@@ -87,7 +87,7 @@ cudaError_t launch_face_flux(int dtype, int rsolver, int64_t nface, int nv, int 
                              const void* Rr, double cs, void* F, cudaStream_t s);
 cudaError_t launch_viscous_flux(int dtype, int ny, int nx, int nv, const void* W, double dx, double dy,
                                 double nu, double smag_cs, int axis, void* out, cudaStream_t s);
-cudaError_t launch_probe(int dtype, int blocks, int iters, double* sink, cudaStream_t s);
+cudaError_t launch_probe(int dtype, int blocks, int iters, int chains, double* sink, cudaStream_t s);
 cudaError_t launch_face_gradients(int dtype, int ny, int nx, int nv, const void* W, double dx, double dy, int axis,
                                   void* gx, void* gy, cudaStream_t s);
 cudaError_t launch_smagorinsky(int dtype, int64_t n, const void* gx, const void* gy, double c, void* out,

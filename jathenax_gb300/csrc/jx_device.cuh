@@ -18,6 +18,17 @@
 // skipped by fmin/fmax, which only matters for a state that has already
 // failed. Single precision uses the native instructions.
 //
+// Float32 arithmetic on the stage path has every rounding explicit
+// (__fmul_rn / __fadd_rn / __fsub_rn / __fmaf_rn through Ops<float>, FMAs
+// placed by hand): the compiler may not fuse a multiply into a neighbouring
+// add on its own, because which pairs it would fuse depends on what else the
+// thread computes (a product shared by two faces of one thread is not fused,
+// the same product alone is). So every float32 kernel variant - shared-memory
+// or register-marching tile, one to three columns per lane, lean or generic
+// form, one solve or a batch - gives the same bits. Float64 keeps the plain
+// operators and the compiler's contraction (its kernels' results are pinned
+// by the parity tests, and its variants share one kernel family per use).
+//
 // Reciprocals and quotients (primitive recovery, Riemann solvers, PLM/PPMX/
 // WENO-Z weights, CFL speeds) go through Num<R>::rcp/div. In float32 both use
 // the special-function unit's approximations (PTX rcp.approx.f32,
@@ -91,11 +102,11 @@ template <> struct Num<float> {
   static __device__ __forceinline__ float div(float a, float b) {
     const unsigned eb = (__float_as_uint(b) >> 23) & 0xff, ea = (__float_as_uint(a) >> 23) & 0xff;
     if (eb == 0 || eb == 0xff || ea == 0xff) return a / b;
-    return a * rcp(b);
+    return __fmul_rn(a, rcp(b));
   }
   static __device__ __forceinline__ float quick_div(float a, float b) { return div(a, b); }
   // sqrt(a) sqrt(b) for a, b >= 0
-  static __device__ __forceinline__ float geo_mean(float a, float b) { return root(a) * root(b); }
+  static __device__ __forceinline__ float geo_mean(float a, float b) { return __fmul_rn(root(a), root(b)); }
 };
 
 template <> struct Num<double> {
@@ -198,6 +209,23 @@ template <> struct Num<double> {
   }
 };
 
+// Explicitly rounded float32 operations (see the file comment); float64 maps
+// to the plain operators, so an expression written with Ops<double> is the
+// same expression the compiler saw before.
+template <typename R> struct Ops;
+template <> struct Ops<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+template <> struct Ops<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+};
+
 // ---------------------------------------------------------------------------
 // Reconstructions (fluxes.py:6-131). PPM4 and PPMX are split into the value
 // at a face, which both neighbouring cells share, and a per-cell limiter
@@ -216,6 +244,8 @@ template <int RECON> struct ReconTraits {
 // Fourth-order interpolant at the face between w1 and w2 (fluxes.py:29-30).
 template <typename R>
 __device__ __forceinline__ R ppm_interp(R w0, R w1, R w2, R w3) {
+  if constexpr (sizeof(R) == 4)
+    return __fmul_rn(__fmaf_rn(7.f, __fadd_rn(w2, w1), -__fadd_rn(w0, w3)), float(1.0 / 12.0));
   return (R(7) * (w2 + w1) - (w0 + w3)) * R(1.0 / 12.0);
 }
 
@@ -254,12 +284,15 @@ __device__ __forceinline__ void ppm4_cell(R c, R lo_face, R hi_face, R& lo, R& h
 template <typename R>
 __device__ __forceinline__ R ppmx_edge(R a, R b, R edge, R ca, R cb) {
   using N = Num<R>;
-  const R curv = R(3) * fma(R(-2), edge, a + b);
+  using O = Ops<R>;
+  const R curv = O::mul(R(3), fma(R(-2), edge, O::add(a, b)));
   const bool agree = (N::gt0(curv) && N::gt0(ca) && N::gt0(cb)) || (N::lt0(curv) && N::lt0(ca) && N::lt0(cb));
   const R mag = N::pmin(fabs(ca), fabs(cb));
-  const R lim = copysign(N::pmin(R(1.25) * mag, fabs(curv)), curv);
-  const R fixed = R(0.5) * (a + b) - (agree ? lim : R(0)) * R(1.0 / 6.0);
-  return N::prod_gt0(a - edge, b - edge) ? fixed : edge;
+  const R lim = copysign(N::pmin(O::mul(R(1.25), mag), fabs(curv)), curv);
+  R fixed;
+  if constexpr (sizeof(R) == 4) fixed = __fmaf_rn(-(agree ? lim : 0.f), float(1.0 / 6.0), __fmul_rn(0.5f, __fadd_rn(a, b)));
+  else fixed = R(0.5) * (a + b) - (agree ? lim : R(0)) * R(1.0 / 6.0);
+  return N::prod_gt0(O::sub(a, edge), O::sub(b, edge)) ? fixed : edge;
 }
 
 // PPMX face value between w1 and w2 (fluxes.py:62-68).
@@ -281,13 +314,13 @@ __device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face
   const R dh = hi_face - c;
   const R dl = lo_face - c;
   const bool ext = N::prod_le0(dh, c - lo_face) || N::prod_le0(m1 - c, c - p1);
-  const R d2 = R(6) * fma(R(-2), c, lo_face + hi_face);
+  const R d2 = Ops<R>::mul(R(6), fma(R(-2), c, lo_face + hi_face));
   const bool agree = (N::gt0(d2) && N::gt0(cl) && N::gt0(cm) && N::gt0(cr)) ||
                      (N::lt0(d2) && N::lt0(cl) && N::lt0(cm) && N::lt0(cr));
   const R mag = N::pmin(fabs(cm), N::pmin(fabs(cl), fabs(cr)));
-  const R lim = copysign(N::pmin(R(1.25) * mag, fabs(d2)), d2);
+  const R lim = copysign(N::pmin(Ops<R>::mul(R(1.25), mag), fabs(d2)), d2);
   const R scale = N::pmax(fabs(m1), N::pmax(fabs(c), fabs(p1)));
-  const bool use = agree && N::pgt(fabs(d2), R(1e-12) * scale);
+  const bool use = agree && N::pgt(fabs(d2), Ops<R>::mul(R(1e-12), scale));
   R ratio = R(0);
   if (use) ratio = N::quick_div(lim, d2);
   const bool steep_lo = N::abs_ge_twice(dl, dh), steep_hi = N::abs_ge_twice(dh, dl);
@@ -302,8 +335,13 @@ __device__ __forceinline__ void ppmx_cell(R m2, R m1, R c, R p1, R p2, R lo_face
     lm = steep_lo ? fma(R(-2), dh, c) : lo_face;
     hm = steep_hi ? fma(R(-2), dl, c) : hi_face;
   }
-  lo = ext ? c + dl * ratio : lm;
-  hi = ext ? c + dh * ratio : hm;
+  if constexpr (sizeof(R) == 4) {
+    lo = ext ? __fmaf_rn(dl, ratio, c) : lm;
+    hi = ext ? __fmaf_rn(dh, ratio, c) : hm;
+  } else {
+    lo = ext ? c + dl * ratio : lm;
+    hi = ext ? c + dh * ratio : hm;
+  }
 }
 
 template <typename R>
@@ -312,10 +350,11 @@ __device__ __forceinline__ void plm_cell(R m1, R c, R p1, R& lo, R& hi) {
   using N = Num<R>;
   const R bw = c - m1;
   const R fw = p1 - c;
+  using O = Ops<R>;
   R hs = R(0);
-  if (N::prod_gt0(bw, fw)) hs = N::quick_div(bw * fw, bw + fw);
-  hi = c + hs;
-  lo = c - hs;
+  if (N::prod_gt0(bw, fw)) hs = N::quick_div(O::mul(bw, fw), O::add(bw, fw));
+  hi = O::add(c, hs);
+  lo = O::sub(c, hs);
 }
 
 // Float64 WENO-Z with every rounding spelled out (explicit FMAs and
@@ -361,43 +400,55 @@ __device__ __forceinline__ void wenoz_cell_f64(double m2, double m1, double c, d
   lo = wenoz_combine_f64(p2, p1, c, m1, m2, w2, w1, w0);
 }
 
-template <typename R>
-__device__ __forceinline__ R wenoz_combine(R s0, R s1, R s2, R s3, R s4, R w0, R w1, R w2) {
+// Float32 (float64 uses wenoz_combine_f64): every rounding explicit.
+__device__ __forceinline__ float wenoz_combine(float s0, float s1, float s2, float s3, float s4, float w0, float w1,
+                                               float w2) {
   // fluxes.py:87-93.
-  const R a0 = R(0.1) * w0, a1 = R(0.6) * w1, a2 = R(0.3) * w2;
-  const R f0 = R(2) * s0 - R(7) * s1 + R(11) * s2;
-  const R f1 = -s1 + R(5) * s2 + R(2) * s3;
-  const R f2 = R(2) * s2 + R(5) * s3 - s4;
-  return Num<R>::div(f0 * a0 + f1 * a1 + f2 * a2, R(6) * (a0 + a1 + a2));
+  const float a0 = __fmul_rn(0.1f, w0), a1 = __fmul_rn(0.6f, w1), a2 = __fmul_rn(0.3f, w2);
+  const float f0 = __fmaf_rn(11.f, s2, __fmaf_rn(-7.f, s1, __fmul_rn(2.f, s0)));
+  const float f1 = __fmaf_rn(2.f, s3, __fmaf_rn(5.f, s2, -s1));
+  const float f2 = __fsub_rn(__fmaf_rn(5.f, s3, __fmul_rn(2.f, s2)), s4);
+  const float num = __fmaf_rn(f2, a2, __fmaf_rn(f1, a1, __fmul_rn(f0, a0)));
+  return Num<float>::div(num, __fmul_rn(6.f, __fadd_rn(__fadd_rn(a0, a1), a2)));
+}
+
+__device__ __forceinline__ void wenoz_cell_f32(float m2, float m1, float c, float p1, float p2, float& lo,
+                                               float& hi) {
+  // fluxes.py:96-117; eps = max(1e-42, finfo(float32).tiny) at fluxes.py:108.
+  using N = Num<float>;
+  const float k1312 = float(13.0 / 12.0);
+  const float eps = 1e-42f > Tiny<float>::value ? 1e-42f : Tiny<float>::value;
+  const float t0 = __fmaf_rn(-2.f, m1, __fadd_rn(m2, c)), u0 = __fmaf_rn(-4.f, m1, __fmaf_rn(3.f, c, m2));
+  const float t1 = __fmaf_rn(-2.f, c, __fadd_rn(m1, p1)), u1 = __fsub_rn(m1, p1);
+  const float t2 = __fmaf_rn(-2.f, p1, __fadd_rn(p2, c)), u2 = __fmaf_rn(-4.f, p1, __fmaf_rn(3.f, c, p2));
+  const float b0 = __fmaf_rn(k1312, __fmul_rn(t0, t0), __fmul_rn(0.25f, __fmul_rn(u0, u0)));
+  const float b1 = __fmaf_rn(k1312, __fmul_rn(t1, t1), __fmul_rn(0.25f, __fmul_rn(u1, u1)));
+  const float b2 = __fmaf_rn(k1312, __fmul_rn(t2, t2), __fmul_rn(0.25f, __fmul_rn(u2, u2)));
+  const float tau = fabsf(__fsub_rn(b0, b2));
+  const float d0 = __fadd_rn(b0, eps), d1 = __fadd_rn(b1, eps), d2 = __fadd_rn(b2, eps);
+  const float dmin = N::pmin(d0, N::pmin(d1, d2));
+  const float inv_sc = N::div(1.f, N::pmax(tau, dmin));
+  float base = __fmul_rn(dmin, inv_sc);
+  base = __fmul_rn(base, base);
+  const float con = __fmul_rn(tau, inv_sc);
+  const float r0 = __fmul_rn(con, N::div(dmin, d0)), r1 = __fmul_rn(con, N::div(dmin, d1)),
+              r2 = __fmul_rn(con, N::div(dmin, d2));
+  const float w0 = __fmaf_rn(r0, r0, base), w1 = __fmaf_rn(r1, r1, base), w2 = __fmaf_rn(r2, r2, base);
+  hi = wenoz_combine(m2, m1, c, p1, p2, w0, w1, w2);
+  lo = wenoz_combine(p2, p1, c, m1, m2, w2, w1, w0);
 }
 
 template <typename R>
 __device__ __forceinline__ void wenoz_cell(R m2, R m1, R c, R p1, R p2, R& lo, R& hi) {
-  if constexpr (sizeof(R) == 8) {
-    wenoz_cell_f64(m2, m1, c, p1, p2, lo, hi);
-    return;
-  }
-  // fluxes.py:96-117; eps = max(1e-42, finfo(dtype).tiny) at fluxes.py:108.
-  using N = Num<R>;
-  const R k1312 = R(13.0 / 12.0);
-  const R eps = R(1e-42) > Tiny<R>::value ? R(1e-42) : Tiny<R>::value;
-  const R t0 = fma(R(-2), m1, m2 + c), u0 = (m2 + R(3) * c) - R(4) * m1;
-  const R t1 = fma(R(-2), c, m1 + p1), u1 = m1 - p1;
-  const R t2 = fma(R(-2), p1, p2 + c), u2 = (p2 + R(3) * c) - R(4) * p1;
-  const R b0 = k1312 * (t0 * t0) + R(0.25) * (u0 * u0);
-  const R b1 = k1312 * (t1 * t1) + R(0.25) * (u1 * u1);
-  const R b2 = k1312 * (t2 * t2) + R(0.25) * (u2 * u2);
-  const R tau = fabs(b0 - b2);
-  const R d0 = b0 + eps, d1 = b1 + eps, d2 = b2 + eps;
-  const R dmin = N::pmin(d0, N::pmin(d1, d2));
-  const R inv_sc = N::div(R(1), N::pmax(tau, dmin));
-  R base = dmin * inv_sc;
-  base = base * base;
-  const R con = tau * inv_sc;
-  const R r0 = con * N::div(dmin, d0), r1 = con * N::div(dmin, d1), r2 = con * N::div(dmin, d2);
-  const R w0 = base + r0 * r0, w1 = base + r1 * r1, w2 = base + r2 * r2;
-  hi = wenoz_combine(m2, m1, c, p1, p2, w0, w1, w2);
-  lo = wenoz_combine(p2, p1, c, m1, m2, w2, w1, w0);
+  if constexpr (sizeof(R) == 8) wenoz_cell_f64(m2, m1, c, p1, p2, lo, hi);
+  else wenoz_cell_f32(m2, m1, c, p1, p2, lo, hi);
+}
+
+// RK4's saved register (hydro.py:46-50 with delta): V + delta U.
+template <typename R>
+__device__ __forceinline__ R delta_update(R v, R delta, R u) {
+  if constexpr (sizeof(R) == 4) return __fmaf_rn(delta, u, v);
+  else return v + delta * u;
 }
 
 // RK stage combine of one component (hydro.py:39-51): the blend form
@@ -457,6 +508,18 @@ __device__ __forceinline__ void flux_llf(R dl, R dr, R ul, R ur, R tl, R tr, con
                                          R& f0, R& f1, R& f2) {
   // fluxes.py:175-183.
   using N = Num<R>;
+  if constexpr (sizeof(R) == 4) {
+    const float ml = __fmul_rn(dl, ul), mr = __fmul_rn(dr, ur);
+    const float ql = __fmul_rn(dl, tl), qr = __fmul_rn(dr, tr);
+    const float s0 = __fadd_rn(ml, mr);
+    const float s1 = __fmaf_rn(ml, ul, __fmaf_rn(mr, ur, __fmul_rn(g.cs2, __fadd_rn(dl, dr))));
+    const float s2 = __fmaf_rn(ml, tl, __fmul_rn(mr, tr));
+    const float sp = N::pmax(__fadd_rn(fabsf(ul), g.cs), __fadd_rn(fabsf(ur), g.cs));
+    f0 = __fmul_rn(0.5f, __fmaf_rn(-sp, __fsub_rn(dr, dl), s0));
+    f1 = __fmul_rn(0.5f, __fmaf_rn(-sp, __fsub_rn(mr, ml), s1));
+    f2 = __fmul_rn(0.5f, __fmaf_rn(-sp, __fsub_rn(qr, ql), s2));
+    return;
+  }
   const R ml = dl * ul, mr = dr * ur;
   const R ql = dl * tl, qr = dr * tr;
   const R s0 = ml + mr;
@@ -475,6 +538,23 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
   using N = Num<R>;
   // Roe average (sl ul + sr ur) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
   // multiplied through by sl: (dl ul + r ur) / (dl + r), r = sqrt(dl dr).
+  if constexpr (sizeof(R) == 4) {
+    const float r = N::geo_mean(dl, dr);
+    const float u = __fmul_rn(__fmaf_rn(r, ur, __fmul_rn(dl, ul)), N::rcp(__fadd_rn(dl, r)));
+    const float alo = N::min(__fsub_rn(u, g.cs), __fsub_rn(ul, g.cs));
+    const float ahi = N::max(__fadd_rn(u, g.cs), __fadd_rn(ur, g.cs));
+    const float bm = N::lt0(alo) ? alo : -1e-20f;
+    const float bp = N::gt0(ahi) ? ahi : 1e-20f;
+    const float vl = __fsub_rn(ul, bm), vr = __fsub_rn(ur, bp);
+    const float ml = __fmul_rn(dl, ul), mr = __fmul_rn(dr, ur);
+    const float fl0 = __fmul_rn(dl, vl), fl1 = __fmaf_rn(ml, vl, __fmul_rn(g.cs2, dl)), fl2 = __fmul_rn(__fmul_rn(dl, tl), vl);
+    const float fr0 = __fmul_rn(dr, vr), fr1 = __fmaf_rn(mr, vr, __fmul_rn(g.cs2, dr)), fr2 = __fmul_rn(__fmul_rn(dr, tr), vr);
+    const float w = N::quick_div(__fmul_rn(0.5f, __fadd_rn(bp, bm)), __fsub_rn(bp, bm));
+    f0 = __fmaf_rn(w, __fsub_rn(fl0, fr0), __fmul_rn(0.5f, __fadd_rn(fl0, fr0)));
+    f1 = __fmaf_rn(w, __fsub_rn(fl1, fr1), __fmul_rn(0.5f, __fadd_rn(fl1, fr1)));
+    f2 = __fmaf_rn(w, __fsub_rn(fl2, fr2), __fmul_rn(0.5f, __fadd_rn(fl2, fr2)));
+    return;
+  }
   const R r = N::geo_mean(dl, dr);
   const R u = fma(r, ur, dl * ul) * N::rcp(dl + r);
   const R alo = N::min(u - g.cs, ul - g.cs);
@@ -490,71 +570,191 @@ __device__ __forceinline__ void flux_hlle(R dl, R dr, R ul, R ur, R tl, R tr, co
   f2 = R(0.5) * (fl2 + fr2) + w * (fl2 - fr2);
 }
 
+// Float32 Roe flux (fluxes.py:134-172), every rounding explicit. The Roe
+// average makes A (U_r - U_l) = F_r - F_l exactly, so with all three wave
+// speeds of one sign the dissipation formula already equals the upwind flux
+// F_l or F_r (fluxes.py:165-166); float32, held to the float64 result only to
+// rounding, relies on that and skips the two selects (four ALU instructions
+// per face in the issue-bound float32 kernels).
+__device__ __forceinline__ void flux_roe_f32(float dl, float dr, float ul, float ur, float tl, float tr,
+                                             const Gas<float>& g, float& f0, float& f1, float& f2) {
+  using N = Num<float>;
+  const float ml = __fmul_rn(dl, ul), mr = __fmul_rn(dr, ur);
+  const float ql = __fmul_rn(dl, tl), qr = __fmul_rn(dr, tr);
+  const float s0 = __fadd_rn(ml, mr);
+  const float s1 = __fmaf_rn(ml, ul, __fmaf_rn(mr, ur, __fmul_rn(g.cs2, __fadd_rn(dl, dr))));
+  const float s2 = __fmaf_rn(ml, tl, __fmul_rn(mr, tr));
+  const float r = N::geo_mean(dl, dr);
+  const float inv = N::rcp(__fadd_rn(dl, r));
+  const float u = __fmul_rn(__fmaf_rn(r, ur, ml), inv);
+  const float t = __fmul_rn(__fmaf_rn(r, tr, ql), inv);
+  const float lm = __fsub_rn(u, g.cs), lp = __fadd_rn(u, g.cs);
+  const float jd = __fsub_rn(dr, dl), jm = __fsub_rn(mr, ml), jq = __fsub_rn(qr, ql);
+  // Wave strengths am = jd (1/2 + u/(2cs)) - jm/(2cs), az = jq - jd t,
+  // ap = jd (1/2 - u/(2cs)) + jm/(2cs) (fluxes.py:150-153).
+  const float hu = __fmul_rn(u, g.half_inv_cs);
+  const float jmc = __fmul_rn(jm, g.half_inv_cs);
+  const float am = __fmaf_rn(jd, __fadd_rn(0.5f, hu), -jmc);
+  const float ap = __fmaf_rn(jd, __fsub_rn(0.5f, hu), jmc);
+  const float az = __fmaf_rn(jd, -t, jq);
+  const float wm = __fmul_rn(fabsf(lm), am), wz = __fmul_rn(fabsf(u), az), wp = __fmul_rn(fabsf(lp), ap);
+  const float wmp = __fadd_rn(wm, wp);
+  const float dstar = __fadd_rn(dl, am);
+  const float dstar2 = __fadd_rn(dstar, ap);
+  if (__builtin_expect(N::lt0(dstar) || N::lt0(dstar2), 0)) {  // positivity fix: rare
+    const float sp = __fmul_rn(0.5f, N::pmax(__fadd_rn(fabsf(ul), g.cs), __fadd_rn(fabsf(ur), g.cs)));
+    f0 = __fmaf_rn(-sp, jd, __fmul_rn(0.5f, s0));
+    f1 = __fmaf_rn(-sp, jm, __fmul_rn(0.5f, s1));
+    f2 = __fmaf_rn(-sp, jq, __fmul_rn(0.5f, s2));
+    return;
+  }
+  f0 = __fmul_rn(0.5f, __fsub_rn(s0, wmp));
+  f1 = __fmul_rn(0.5f, __fsub_rn(s1, __fmaf_rn(wm, lm, __fmul_rn(wp, lp))));
+  f2 = __fmul_rn(0.5f, __fsub_rn(s2, __fmaf_rn(wmp, t, wz)));
+}
+
 template <typename R>
 __device__ __forceinline__ void flux_roe(R dl, R dr, R ul, R ur, R tl, R tr, const Gas<R>& g,
                                          R& f0, R& f1, R& f2) {
   // fluxes.py:134-172.
-  using N = Num<R>;
-  const R ml = dl * ul, mr = dr * ur;
-  const R ql = dl * tl, qr = dr * tr;
-  const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
-  const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
-  // Roe averages (sl v_l + sr v_r) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
-  // multiplied through by sl: (dl v_l + r v_r) / (dl + r), r = sqrt(dl dr).
-  const R r = N::geo_mean(dl, dr);
-  const R inv = N::rcp(dl + r);
-  const R u = fma(r, ur, ml) * inv;
-  const R t = fma(r, tr, ql) * inv;
-  const R lm = u - g.cs, lp = u + g.cs;
-  const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
-  // Wave strengths am = jd (1/2 + u/(2cs)) - jm/(2cs), az = jq - jd t,
-  // ap = jd (1/2 - u/(2cs)) + jm/(2cs) (fluxes.py:150-153);
-  // g = (l + r)/2 - (|lm| am e_m + |u| az e_z + |lp| ap e_p)/2 with the
-  // eigenvectors e_m = (1, lm, t), e_z = (0, 0, 1), e_p = (1, lp, t).
-  // In float64 am, ap and |u| az are formed halved and each component of g
-  // is one FMA (two float64 operations fewer per face). Float32 keeps the
-  // direct form, which measured faster in the marching kernel.
-  const R s0 = l0 + r0, s1 = l1 + r1, s2 = l2 + r2;
-  const R az = fma(jd, -t, jq);
-  R g0, g1, g2, dstar, dstar2;
-  if constexpr (sizeof(R) == 8) {
-    // am = jd/2 + X/(2cs), ap = jd/2 - X/(2cs) with X = u jd - jm: one FMA
-    // for X serves both (two float64 operations fewer per face).
+  if constexpr (sizeof(R) == 4) {
+    flux_roe_f32(dl, dr, ul, ur, tl, tr, g, f0, f1, f2);
+  } else {
+    using N = Num<R>;
+    const R ml = dl * ul, mr = dr * ur;
+    const R ql = dl * tl, qr = dr * tr;
+    const R l0 = ml, l1 = ml * ul + g.cs2 * dl, l2 = ml * tl;
+    const R r0 = mr, r1 = mr * ur + g.cs2 * dr, r2 = mr * tr;
+    // Roe averages (sl v_l + sr v_r) / (sl + sr), sl = sqrt(dl), sr = sqrt(dr),
+    // multiplied through by sl: (dl v_l + r v_r) / (dl + r), r = sqrt(dl dr).
+    const R r = N::geo_mean(dl, dr);
+    const R inv = N::rcp(dl + r);
+    const R u = fma(r, ur, ml) * inv;
+    const R t = fma(r, tr, ql) * inv;
+    const R lm = u - g.cs, lp = u + g.cs;
+    const R jd = dr - dl, jm = mr - ml, jq = qr - ql;
+    // Wave strengths am = jd (1/2 + u/(2cs)) - jm/(2cs), az = jq - jd t,
+    // ap = jd (1/2 - u/(2cs)) + jm/(2cs) (fluxes.py:150-153);
+    // g = (l + r)/2 - (|lm| am e_m + |u| az e_z + |lp| ap e_p)/2 with the
+    // eigenvectors e_m = (1, lm, t), e_z = (0, 0, 1), e_p = (1, lp, t).
+    // am, ap and |u| az are formed halved and each component of g is one FMA
+    // (two float64 operations fewer per face); am = jd/2 + X/(2cs),
+    // ap = jd/2 - X/(2cs) with X = u jd - jm: one FMA for X serves both (two
+    // float64 operations fewer per face).
+    const R s0 = l0 + r0, s1 = l1 + r1, s2 = l2 + r2;
+    const R az = fma(jd, -t, jq);
     const R X = fma(u, jd, -jm);
     const R jq4 = R(0.25) * jd;
     const R am = fma(X, g.quarter_inv_cs, jq4);   // am / 2
     const R ap = fma(-X, g.quarter_inv_cs, jq4);  // ap / 2
     const R wm = fabs(lm) * am, wz = (R(0.5) * fabs(u)) * az, wp = fabs(lp) * ap;  // halves
     const R wmp = wm + wp;
-    g0 = fma(R(0.5), s0, -wmp);
-    g1 = fma(R(0.5), s1, -fma(wm, lm, wp * lp));
-    g2 = fma(R(0.5), s2, -fma(wmp, t, wz));
-    dstar = fma(R(2), am, dl);  // dl + am
-    dstar2 = fma(R(2), ap, dstar);
+    R g0 = fma(R(0.5), s0, -wmp);
+    R g1 = fma(R(0.5), s1, -fma(wm, lm, wp * lp));
+    R g2 = fma(R(0.5), s2, -fma(wmp, t, wz));
+    const R dstar = fma(R(2), am, dl);  // dl + am
+    const R dstar2 = fma(R(2), ap, dstar);
+    // Supersonic faces take the upwind flux (fluxes.py:165-166).
+    if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
+    if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
+    if (__builtin_expect(N::lt0(dstar) || N::lt0(dstar2), 0)) {  // positivity fix: rare
+      const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
+      g0 = R(0.5) * s0 - sp * jd;
+      g1 = R(0.5) * s1 - sp * jm;
+      g2 = R(0.5) * s2 - sp * jq;
+    }
+    f0 = g0;
+    f1 = g1;
+    f2 = g2;
+  }
+}
+
+// Viscous momentum flux at a face (fluxes.py:227-266), added to (f1, f2):
+// DIR 0 an x face, DIR 1 a y face, between cell a (low side) and cell b
+// (high side) with velocities (ax, ay), (bx, by) and densities rho_a,
+// rho_b; (tpx, tpy) and (tmx, tmy) are the transverse sums (b+ + a+) and
+// (b- + a-) of the velocity one cell beyond the face on either side.
+// inv_dn = 1/dx (x face) or 1/dy, inv_4dt = 1/(4 dy) or 1/(4 dx); nu the
+// uniform viscosity, smag_c = Cs^2 dx dy (Smagorinsky when smag).
+template <int DIR, typename R>
+__device__ __forceinline__ void viscous_face(bool smag, R nu0, R smag_c, R inv_dn, R inv_4dt, R rho_a, R rho_b,
+                                             R ax, R ay, R bx, R by, R tpx, R tpy, R tmx, R tmy, R& f1, R& f2) {
+  if constexpr (sizeof(R) == 4) {
+    const float dn_x = __fmul_rn(__fsub_rn(bx, ax), inv_dn), dn_y = __fmul_rn(__fsub_rn(by, ay), inv_dn);
+    const float dt_x = __fmul_rn(__fsub_rn(tpx, tmx), inv_4dt), dt_y = __fmul_rn(__fsub_rn(tpy, tmy), inv_4dt);
+    const float dvx_dx = DIR == 0 ? dn_x : dt_x, dvy_dx = DIR == 0 ? dn_y : dt_y;
+    const float dvx_dy = DIR == 0 ? dt_x : dn_x, dvy_dy = DIR == 0 ? dt_y : dn_y;
+    const float shear = __fadd_rn(dvy_dx, dvx_dy);
+    const float s0 = DIR == 0 ? __fmaf_rn(float(4.0 / 3.0), dvx_dx, -__fmul_rn(float(2.0 / 3.0), dvy_dy)) : shear;
+    const float s1 = DIR == 0 ? shear : __fmaf_rn(float(4.0 / 3.0), dvy_dy, -__fmul_rn(float(2.0 / 3.0), dvx_dx));
+    float nu = nu0;
+    if (smag) {
+      const float s2 = __fmaf_rn(shear, shear, __fmul_rn(2.f, __fmaf_rn(dvx_dx, dvx_dx, __fmul_rn(dvy_dy, dvy_dy))));
+      nu = __fmaf_rn(smag_c, sqrtf(s2), nu);
+    }
+    const float mu = __fmul_rn(__fmul_rn(0.5f, nu), __fadd_rn(rho_b, rho_a));
+    f1 = __fmaf_rn(-mu, s0, f1);
+    f2 = __fmaf_rn(-mu, s1, f2);
   } else {
-    const R hu = u * g.half_inv_cs;  // (u / 2) / cs
-    const R jmc = jm * g.half_inv_cs;
-    const R am = fma(jd, R(0.5) + hu, -jmc);
-    const R ap = fma(jd, R(0.5) - hu, jmc);
-    const R wm = fabs(lm) * am, wz = fabs(u) * az, wp = fabs(lp) * ap;
-    const R wmp = wm + wp;
-    g0 = R(0.5) * (s0 - wmp);
-    g1 = R(0.5) * (s1 - fma(wm, lm, wp * lp));
-    g2 = R(0.5) * (s2 - fma(wmp, t, wz));
-    dstar = dl + am;
-    dstar2 = dstar + ap;
+    R dvx_dx, dvy_dx, dvx_dy, dvy_dy;
+    if (DIR == 0) {
+      dvx_dx = (bx - ax) * inv_dn;
+      dvy_dx = (by - ay) * inv_dn;
+      dvx_dy = (tpx - tmx) * inv_4dt;
+      dvy_dy = (tpy - tmy) * inv_4dt;
+    } else {
+      dvx_dy = (bx - ax) * inv_dn;
+      dvy_dy = (by - ay) * inv_dn;
+      dvx_dx = (tpx - tmx) * inv_4dt;
+      dvy_dx = (tpy - tmy) * inv_4dt;
+    }
+    const R shear = dvy_dx + dvx_dy;
+    R s0, s1;
+    if (DIR == 0) {
+      s0 = R(4.0 / 3.0) * dvx_dx - R(2.0 / 3.0) * dvy_dy;
+      s1 = shear;
+    } else {
+      s0 = shear;
+      s1 = R(4.0 / 3.0) * dvy_dy - R(2.0 / 3.0) * dvx_dx;
+    }
+    R nu = nu0;
+    if (smag) {
+      const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + shear * shear;
+      nu = nu + smag_c * sqrt(s2);
+    }
+    const R mu = (R(0.5) * nu) * (rho_b + rho_a);
+    f1 = f1 + -(mu * s0);
+    f2 = f2 + -(mu * s1);
   }
-  if (N::ge0(lm)) { g0 = l0; g1 = l1; g2 = l2; }
-  if (N::le0(lp)) { g0 = r0; g1 = r1; g2 = r2; }
-  if (__builtin_expect(N::lt0(dstar) || N::lt0(dstar2), 0)) {  // positivity fix: rare
-    const R sp = R(0.5) * N::pmax(fabs(ul) + g.cs, fabs(ur) + g.cs);
-    g0 = R(0.5) * s0 - sp * jd;
-    g1 = R(0.5) * s1 - sp * jm;
-    g2 = R(0.5) * s2 - sp * jq;
-  }
-  f0 = g0;
-  f1 = g1;
-  f2 = g2;
+}
+
+// Half the sum of two face-adjacent SGS stress values added to a flux
+// component (fluxes.py:269-280).
+template <typename R>
+__device__ __forceinline__ R add_half_sum(R f, R ta, R tb) {
+  if constexpr (sizeof(R) == 4) return __fmaf_rn(0.5f, __fadd_rn(ta, tb), f);
+  else return f + R(0.5) * (ta + tb);
+}
+
+// Passive-scalar flux: the mass flux times the upwind concentration
+// (fluxes.py:215-218).
+template <typename R>
+__device__ __forceinline__ R scalar_flux(R f0, R left, R right) {
+  return Ops<R>::mul(f0, Num<R>::ge0(f0) ? left : right);
+}
+
+// Linear drag on one momentum component with the incoming density and
+// velocity (hydro.py:122-125): m - (beta dt rate rho) v.
+template <typename R>
+__device__ __forceinline__ R drag_term(R m, R kdrag_rho, R v) {
+  if constexpr (sizeof(R) == 4) return __fmaf_rn(-kdrag_rho, v, m);
+  else return m + -(kdrag_rho * v);
+}
+
+// CFL signal speed |m / rho| + cs with inv = 1/rho.
+template <typename R>
+__device__ __forceinline__ R signal_speed(R inv, R m, R cs) {
+  return Ops<R>::add(fabs(Ops<R>::mul(inv, m)), cs);
 }
 
 template <int RS, typename R>

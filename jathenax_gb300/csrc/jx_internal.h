@@ -42,6 +42,7 @@ struct StageParams {
   WsHeader* header;
   jx_trace trace;
   int ny, nx, nv, tx, ty, tiles_x;
+  int nc;  // marching kernel: columns per lane (tx = 32 nc - 6)
   double dx, dy, inv_dx, inv_dy, inv_4dx, inv_4dy;
   double cs, dfloor, nu, smag_c, drag;
   double g0, g1, beta, delta;
@@ -113,29 +114,38 @@ inline size_t fast_smem_bytes(int recon, int dtype, int ty) {
 }
 
 // Register-marching stage kernel (jx_stage_march.cuh): one warp per tile of
-// kMarchTileX columns by StageParams::ty rows (two columns per lane, 3 ghost
-// columns per side of the 64-column strip). Blocks are single warps: the
-// warps share nothing, and the SM's register file then holds as many warps
-// as registers allow (no rounding to whole multi-warp blocks).
+// march_tile_x(nc) columns by StageParams::ty rows (nc = 1, 2 or 3 columns
+// per lane, 3 ghost columns per side of the 32 nc-column strip); the default
+// is two columns (58-column tiles). Blocks are single warps: the warps share
+// nothing, and the SM's register file then holds as many warps as registers
+// allow (no rounding to whole multi-warp blocks).
 constexpr int kMarchWarps = 1;
-constexpr int kMarchTileX = 58;
+__host__ __device__ constexpr int march_tile_x(int nc) { return 32 * nc - 6; }
+constexpr int kMarchTileX = march_tile_x(2);
 constexpr int kMarchMinRows = 8;
+// Columns per lane of a marching tile width (0: not a marching width).
+inline int march_cols(int tile_x) {
+  for (int nc = 1; nc <= 3; ++nc)
+    if (tile_x == march_tile_x(nc)) return nc;
+  return 0;
+}
 
 cudaError_t launch_march_dc(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_plm(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_ppm4(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_ppmx(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_wenoz(int, int, const StageParams&, dim3, cudaStream_t);
-cudaError_t launch_batch_march_dc(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_plm(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppm4(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppmx(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_wenoz(int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, bool batch);
-int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, bool batch);
-int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, bool batch);
-int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, bool batch);
-int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, bool batch);
+// (dtype, rsolver, nv, nc, params, tile offsets, nsolves, nwork, grid, stream)
+cudaError_t launch_batch_march_dc(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_plm(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppm4(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppmx(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_wenoz(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch);
+int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch);
+int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, bool batch);
+int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, int nc, bool batch);
+int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, int nc, bool batch);
 
 typedef cudaError_t (*FaceStatesLauncher)(int dtype, const void* W, int ny, int nx, int nv,
                                           int axis, double dfloor, void* left, void* right,

@@ -144,35 +144,11 @@ __device__ __forceinline__ void sweep(const StageParams& p, const StageConsts<R>
         const int sa = sb - S::stride(PW);
         const R* vx = t.W + t.wplane;
         const R* vy = t.W + 2 * t.wplane;
-        R dvx_dx, dvy_dx, dvx_dy, dvy_dy;
-        if (DIR == 0) {
-          dvx_dx = (vx[sb] - vx[sa]) * k.inv_dx;
-          dvy_dx = (vy[sb] - vy[sa]) * k.inv_dx;
-          dvx_dy = ((vx[sb + PW] + vx[sa + PW]) - (vx[sb - PW] + vx[sa - PW])) * k.inv_4dy;
-          dvy_dy = ((vy[sb + PW] + vy[sa + PW]) - (vy[sb - PW] + vy[sa - PW])) * k.inv_4dy;
-        } else {
-          dvx_dy = (vx[sb] - vx[sa]) * k.inv_dy;
-          dvy_dy = (vy[sb] - vy[sa]) * k.inv_dy;
-          dvx_dx = ((vx[sb + 1] + vx[sa + 1]) - (vx[sb - 1] + vx[sa - 1])) * k.inv_4dx;
-          dvy_dx = ((vy[sb + 1] + vy[sa + 1]) - (vy[sb - 1] + vy[sa - 1])) * k.inv_4dx;
-        }
-        const R shear = dvy_dx + dvx_dy;
-        R s0, s1;
-        if (DIR == 0) {
-          s0 = R(4.0 / 3.0) * dvx_dx - R(2.0 / 3.0) * dvy_dy;
-          s1 = shear;
-        } else {
-          s0 = shear;
-          s1 = R(4.0 / 3.0) * dvy_dy - R(2.0 / 3.0) * dvx_dx;
-        }
-        R nu = k.nu;
-        if (p.smag_on) {
-          const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + shear * shear;
-          nu = nu + k.smag_c * sqrt(s2);
-        }
-        const R mu = (R(0.5) * nu) * (t.W[sb] + t.W[sa]);
-        f1 = f1 + -(mu * s0);
-        f2 = f2 + -(mu * s1);
+        const int ts = DIR == 0 ? PW : 1;  // transverse neighbours
+        viscous_face<DIR, R>(p.smag_on, k.nu, k.smag_c, DIR == 0 ? k.inv_dx : k.inv_dy,
+                             DIR == 0 ? k.inv_4dy : k.inv_4dx, t.W[sa], t.W[sb], vx[sa], vy[sa], vx[sb], vy[sb],
+                             vx[sb + ts] + vx[sa + ts], vy[sb + ts] + vy[sa + ts], vx[sb - ts] + vx[sa - ts],
+                             vy[sb - ts] + vy[sa - ts], f1, f2);
       }
       if (tau != nullptr) {
         const int gy = wrap_index(y0 + r, p.ny), gx = wrap_index(x0 + c, p.nx);
@@ -181,8 +157,8 @@ __device__ __forceinline__ void sweep(const StageParams& p, const StageConsts<R>
         const R* tb = tau + ((size_t)gy * p.nx + gx) * 3;
         const R* ta = tau + ((size_t)ay * p.nx + ax) * 3;
         constexpr int k0 = DIR == 0 ? 0 : 1;
-        f1 = f1 + R(0.5) * (ta[k0] + tb[k0]);
-        f2 = f2 + R(0.5) * (ta[k0 + 1] + tb[k0 + 1]);
+        f1 = add_half_sum(f1, ta[k0], tb[k0]);
+        f2 = add_half_sum(f2, ta[k0 + 1], tb[k0 + 1]);
       }
 
       const bool own = q < n;  // the low face of a cell of this tile
@@ -200,7 +176,7 @@ __device__ __forceinline__ void sweep(const StageParams& p, const StageConsts<R>
       L[2 * fplane] = f2;
       for (int v = 3; v < NV; ++v) {
         const R up = Num<R>::ge0(f0) ? L[v * fplane] : Rr[v * t.rplane];
-        L[v * fplane] = f0 * up;
+        L[v * fplane] = Ops<R>::mul(f0, up);
       }
       if (p.trace_on && own) {
         R* tf = static_cast<R*>(DIR == 0 ? p.trace.flux_x : p.trace.flux_y);
@@ -259,7 +235,7 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
     const R inv = Num<R>::rcp(rho);
     const int s = ly * PW + lx;
     t.W[s] = rho;
-    for (int v = 1; v < NV; ++v) t.W[v * t.wplane + s] = inv * u[v];
+    for (int v = 1; v < NV; ++v) t.W[v * t.wplane + s] = Ops<R>::mul(inv, u[v]);
   }
   __syncthreads();
 
@@ -287,11 +263,11 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
       R vs = V[cell + v];
       if (v == 0 && p.floor_v) vs = N::lt(vs, k.dfloor) ? k.dfloor : vs;
       if (p.has_delta) {
-        vs = vs + k.delta * u;
+        vs = delta_update(vs, k.delta, u);
         if (Vo) Vo[cell + v] = vs;
       }
       R un = rk_combine<R>(p.blend, k.g0, k.g1, u, vs, t.Fx[fx + 1] - t.Fx[fx], t.Fy[fy + TX] - t.Fy[fy], ncx, ncy);
-      if (p.drag_on && (v == 1 || v == 2)) un = un + -((kdrag * rho_in) * t.W[v * t.wplane + sw]);
+      if (p.drag_on && (v == 1 || v == 2)) un = drag_term(un, kdrag * rho_in, t.W[v * t.wplane + sw]);
       if (p.trace_on) {
         if (p.trace.saved) static_cast<R*>(p.trace.saved)[cell + v] = vs;
         if (p.trace.conserved) static_cast<R*>(p.trace.conserved)[cell + v] = un;
@@ -310,8 +286,8 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageParams 
     if (p.want_cfl) {
       // Both candidates are >= cs > 0 or NaN: an ordered max that keeps NaN.
       const R inv = Num<R>::rcp(out0);
-      vmax0 = N::nanmax_pos(vmax0, fabs(inv * out1) + k.cs);
-      vmax1 = N::nanmax_pos(vmax1, fabs(inv * out2) + k.cs);
+      vmax0 = N::nanmax_pos(vmax0, signal_speed(inv, out1, k.cs));
+      vmax1 = N::nanmax_pos(vmax1, signal_speed(inv, out2, k.cs));
     }
   }
   if (p.want_cfl) {

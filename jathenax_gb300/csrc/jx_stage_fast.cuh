@@ -195,38 +195,14 @@ __device__ __forceinline__ void fast_sweep(const StageParams& p, const StageCons
       if (p.visc_on) {
         const int sb = (r + H) * PW + (c + H);
         const int sa = sb - ST;
-        R dvx_dx, dvy_dx, dvx_dy, dvy_dy;
         const Cell4<R> b = t.W[sb], a = t.W[sa];
-        if (DIR == 0) {
-          const Cell4<R> bu = t.W[sb + PW], au = t.W[sa + PW], bd = t.W[sb - PW], ad = t.W[sa - PW];
-          dvx_dx = (b.v[1] - a.v[1]) * k.inv_dx;
-          dvy_dx = (b.v[2] - a.v[2]) * k.inv_dx;
-          dvx_dy = ((bu.v[1] + au.v[1]) - (bd.v[1] + ad.v[1])) * k.inv_4dy;
-          dvy_dy = ((bu.v[2] + au.v[2]) - (bd.v[2] + ad.v[2])) * k.inv_4dy;
-        } else {
-          const Cell4<R> bp = t.W[sb + 1], ap = t.W[sa + 1], bm = t.W[sb - 1], am = t.W[sa - 1];
-          dvx_dy = (b.v[1] - a.v[1]) * k.inv_dy;
-          dvy_dy = (b.v[2] - a.v[2]) * k.inv_dy;
-          dvx_dx = ((bp.v[1] + ap.v[1]) - (bm.v[1] + am.v[1])) * k.inv_4dx;
-          dvy_dx = ((bp.v[2] + ap.v[2]) - (bm.v[2] + am.v[2])) * k.inv_4dx;
-        }
-        const R shear = dvy_dx + dvx_dy;
-        R s0, s1;
-        if (DIR == 0) {
-          s0 = R(4.0 / 3.0) * dvx_dx - R(2.0 / 3.0) * dvy_dy;
-          s1 = shear;
-        } else {
-          s0 = shear;
-          s1 = R(4.0 / 3.0) * dvy_dy - R(2.0 / 3.0) * dvx_dx;
-        }
-        R nu = k.nu;
-        if (p.smag_on) {
-          const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + shear * shear;
-          nu = nu + k.smag_c * sqrt(s2);
-        }
-        const R mu = (R(0.5) * nu) * (b.v[0] + a.v[0]);
-        f.v[1] = f.v[1] + -(mu * s0);
-        f.v[2] = f.v[2] + -(mu * s1);
+        // Transverse neighbours one cell beyond the face on either side.
+        constexpr int TS = DIR == 0 ? PW : 1;
+        const Cell4<R> bp = t.W[sb + TS], ap = t.W[sa + TS], bm = t.W[sb - TS], am = t.W[sa - TS];
+        viscous_face<DIR, R>(p.smag_on, k.nu, k.smag_c, DIR == 0 ? k.inv_dx : k.inv_dy,
+                             DIR == 0 ? k.inv_4dy : k.inv_4dx, a.v[0], b.v[0], a.v[1], a.v[2], b.v[1], b.v[2],
+                             bp.v[1] + ap.v[1], bp.v[2] + ap.v[2], bm.v[1] + am.v[1], bm.v[2] + am.v[2], f.v[1],
+                             f.v[2]);
       }
       if (tau != nullptr) {
         const int gy = wrap_fast(y0 + r, p.ny), gx = wrap_fast(x0 + c, p.nx);
@@ -235,11 +211,11 @@ __device__ __forceinline__ void fast_sweep(const StageParams& p, const StageCons
         const R* tb = tau + ((size_t)gy * p.nx + gx) * 3;
         const R* ta = tau + ((size_t)ay * p.nx + ax) * 3;
         constexpr int k0 = DIR == 0 ? 0 : 1;
-        f.v[1] = f.v[1] + R(0.5) * (ta[k0] + tb[k0]);
-        f.v[2] = f.v[2] + R(0.5) * (ta[k0 + 1] + tb[k0 + 1]);
+        f.v[1] = add_half_sum(f.v[1], ta[k0], tb[k0]);
+        f.v[2] = add_half_sum(f.v[2], ta[k0 + 1], tb[k0 + 1]);
       }
 #pragma unroll
-      for (int v = 3; v < NV; ++v) f.v[v] = f0 * (N::ge0(f0) ? L.v[v] : Rv.v[v]);
+      for (int v = 3; v < NV; ++v) f.v[v] = scalar_flux(f0, L.v[v], Rv.v[v]);
       if (p.trace_on && q < n && y0 + r < p.ny && x0 + c < p.nx) {
         const size_t cell = (size_t)(y0 + r) * p.nx + (x0 + c);
         store_cell_scalar<R, NV>(DIR == 0 ? p.trace.left_x : p.trace.left_y, cell, L);
@@ -292,7 +268,7 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
     const R inv = Num<R>::rcp(rho);
     w.v[0] = rho;
 #pragma unroll
-    for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? inv * u.v[v] : R(0);
+    for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? Ops<R>::mul(inv, u.v[v]) : R(0);
     t.W[idx] = w;
   }
   __syncthreads();
@@ -329,14 +305,14 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
       Cell4<R> un;
   #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        if (kDelta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
+        if (kDelta) vs.v[v] = delta_update(vs.v[v], k.delta, u.v[v]);
         un.v[v] = rk_combine<R>(kBlend, k.g0, k.g1, u.v[v], vs.v[v], fxr.v[v] - fxl.v[v], fyr.v[v] - fyl.v[v], ncx,
                                 ncy);
       }
       un.v[3] = NV == 4 ? un.v[3] : R(0);
       if (kDrag) {
-        un.v[1] = un.v[1] + -((kdrag * w.v[0]) * w.v[1]);
-        un.v[2] = un.v[2] + -((kdrag * w.v[0]) * w.v[2]);
+        un.v[1] = drag_term(un.v[1], kdrag * w.v[0], w.v[1]);
+        un.v[2] = drag_term(un.v[2], kdrag * w.v[0], w.v[2]);
       }
       if (p.trace_on) {
         store_cell_scalar<R, NV>(p.trace.saved, cell, vs);
@@ -348,8 +324,8 @@ __device__ __forceinline__ void fast_tile(const StageParams& p, int tile, int nt
       store_cell<R, NV>(Uo + cell * NV, un);
       if (kCfl) {
         const R inv = Num<R>::rcp(un.v[0]);
-        vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
-        vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
+        vmax0 = N::nanmax_pos(vmax0, signal_speed(inv, un.v[1], k.cs));
+        vmax1 = N::nanmax_pos(vmax1, signal_speed(inv, un.v[2], k.cs));
       }
     }
   };

@@ -25,6 +25,8 @@
 #include "jx_internal.h"
 #include "jx_stage_fast.cuh"
 
+#include <utility>
+
 namespace jx {
 
 template <typename R, int NV>
@@ -50,7 +52,7 @@ __device__ __forceinline__ Cell4<R> recover_cell(const Cell4<R>& u, R dfloor) {
   const R inv = Num<R>::rcp(rho);
   w.v[0] = rho;
 #pragma unroll
-  for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? inv * u.v[v] : R(0);
+  for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? Ops<R>::mul(inv, u.v[v]) : R(0);
   return w;
 }
 
@@ -92,7 +94,7 @@ __device__ __forceinline__ Cell4<R> face_flux_cells(const Cell4<R>& L, const Cel
   f.v[2] = DIR == 0 ? ft : fn;
   f.v[3] = R(0);
 #pragma unroll
-  for (int v = 3; v < NV; ++v) f.v[v] = f0 * (Num<R>::ge0(f0) ? L.v[v] : Rv.v[v]);
+  for (int v = 3; v < NV; ++v) f.v[v] = scalar_flux(f0, L.v[v], Rv.v[v]);
   return f;
 }
 
@@ -102,67 +104,104 @@ __device__ __forceinline__ Cell4<R> face_flux_cells(const Cell4<R>& L, const Cel
 template <int DIR, typename R>
 __device__ __forceinline__ void viscous_add(const StageParams& p, const StageConsts<R>& k, R rho_a, R rho_b,
                                             R ax, R ay, R bx, R by, R tpx, R tpy, R tmx, R tmy, Cell4<R>& f) {
-  R dvx_dx, dvy_dx, dvx_dy, dvy_dy;
-  if (DIR == 0) {
-    dvx_dx = (bx - ax) * k.inv_dx;
-    dvy_dx = (by - ay) * k.inv_dx;
-    dvx_dy = (tpx - tmx) * k.inv_4dy;
-    dvy_dy = (tpy - tmy) * k.inv_4dy;
-  } else {
-    dvx_dy = (bx - ax) * k.inv_dy;
-    dvy_dy = (by - ay) * k.inv_dy;
-    dvx_dx = (tpx - tmx) * k.inv_4dx;
-    dvy_dx = (tpy - tmy) * k.inv_4dx;
-  }
-  const R shear = dvy_dx + dvx_dy;
-  R s0, s1;
-  if (DIR == 0) {
-    s0 = R(4.0 / 3.0) * dvx_dx - R(2.0 / 3.0) * dvy_dy;
-    s1 = shear;
-  } else {
-    s0 = shear;
-    s1 = R(4.0 / 3.0) * dvy_dy - R(2.0 / 3.0) * dvx_dx;
-  }
-  R nu = k.nu;
-  if (p.smag_on) {
-    const R s2 = R(2) * (dvx_dx * dvx_dx + dvy_dy * dvy_dy) + shear * shear;
-    nu = nu + k.smag_c * sqrt(s2);
-  }
-  const R mu = (R(0.5) * nu) * (rho_b + rho_a);
-  f.v[1] = f.v[1] + -(mu * s0);
-  f.v[2] = f.v[2] + -(mu * s1);
+  viscous_face<DIR, R>(p.smag_on, k.nu, k.smag_c, DIR == 0 ? k.inv_dx : k.inv_dy, DIR == 0 ? k.inv_4dy : k.inv_4dx,
+                       rho_a, rho_b, ax, ay, bx, by, tpx, tpy, tmx, tmy, f.v[1], f.v[2]);
 }
 
-// Both columns of one lane: a 5-row window of primitives (rows j-4 .. j),
-// the face value below row j-1, the upper edge of row j-3 and the y flux
-// below row j-3 (see the file comment).
+// One column of a lane: a 5-row window of primitives (rows j-4 .. j), the
+// face value below row j-1, the upper edge of row j-3 and the y flux below
+// row j-3 (see the file comment).
 template <typename R> struct MarchColumn {
   Cell4<R> W4, W3, W2, W1, W0, Ay2, hy3, Fy3;
 };
+
+// Compile-time form of a marching launch. kMarchGeneric reads every stage
+// option from StageParams at run time; the two lean forms are the stages of
+// a problem without viscosity, SGS stress or drag (the inviscid runs) with
+// the RK combine's blend form fixed, so that the walk carries no viscous
+// window row and tests no per-launch flag in its steady state.
+enum MarchForm { kMarchGeneric = 0, kMarchLeanPlain = 1, kMarchLeanBlend = 2 };
+
+// The cell at column c0 + K of the lane's row, K in [-2, NC + 1]: one of
+// the lane's own NC columns, or a neighbouring lane's by a warp shuffle.
+template <int K, int NC, typename R, int NV>
+__device__ __forceinline__ Cell4<R> lane_cell(const Cell4<R> (&own)[NC]) {
+  if constexpr (K >= 0 && K < NC) {
+    return own[K];
+  } else if constexpr (K < 0) {
+    constexpr int back = (-K + NC - 1) / NC;
+    return shfl_up_cell<R, NV>(own[K + back * NC], back);
+  } else {
+    constexpr int ahead = K / NC;
+    return shfl_down_cell<R, NV>(own[K - ahead * NC], ahead);
+  }
+}
+
+template <int NC, typename R, int NV, int... I>
+__device__ __forceinline__ void lane_cells_impl(const Cell4<R> (&own)[NC], Cell4<R> (&E)[NC + 4],
+                                                std::integer_sequence<int, I...>) {
+  ((E[I] = lane_cell<I - 2, NC, R, NV>(own)), ...);
+}
+
+// E[k + 2] = the cell at column c0 + k, k = -2 .. NC + 1.
+template <int NC, typename R, int NV>
+__device__ __forceinline__ void lane_cells(const Cell4<R> (&own)[NC], Cell4<R> (&E)[NC + 4]) {
+  lane_cells_impl<NC, R, NV>(own, E, std::make_integer_sequence<int, NC + 4>{});
+}
 
 // PREFETCH_V: issue L2 prefetches of the saved register two rows ahead of
 // the RK combine. Measured on GB300: it helps the batch kernel (12 resident
 // warps per SM, ensemble cycle -2.2 %) and costs the single-solve kernel
 // (16 warps, already hiding the latency; +2.4 % at 4096²). Results do not
 // depend on it.
-template <typename R, int RECON, int RS, int NV, bool PREFETCH_V>
+//
+// NC columns per lane: lane l holds columns c0 .. c0 + NC - 1 of a strip of
+// 32 NC columns (c0 = x0 - 3 + NC l), of which the middle 32 NC - 6 are the
+// tile's outputs. Every cell's arithmetic is the same whatever NC is, so
+// results do not depend on it.
+//
+// The walk is a 6-row prologue (the rows above the tile's first output row
+// only feed the y sweep) and a steady loop in which every phase runs and no
+// phase is tested. The steady loop is deliberately not unrolled: unrolling it
+// by 2, 3 or 5 (so that the register window would shift by renaming instead
+// of moves) measured 5, 12 and 34 % slower on GB300, the body outgrowing the
+// instruction cache. Lanes whose columns are ghosts (or beyond a ragged right
+// edge) run the RK combine on a cell of their own tile and skip only the
+// store, so the combine has no divergent branch.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM, bool PREFETCH_V>
 __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int ntiles) {
   using N = Num<R>;
+  constexpr bool kLean = FORM != kMarchGeneric;
+  constexpr int TX = march_tile_x(NC);
   const StageConsts<R>& k = stage_consts<R>(p);
   const int lane = threadIdx.x & 31;
   const int TY = p.ty;
   const int bx = tile % p.tiles_x, by = tile / p.tiles_x;
-  const int x0 = bx * kMarchTileX;  // first output column of the tile
+  const int x0 = bx * TX;  // first output column of the tile
   const int y0 = by * TY;
-  const int c0 = x0 - 3 + 2 * lane;  // this lane's columns: c0 and c0 + 1
-  const int gx[2] = {wrap_fast(c0, p.nx), wrap_fast(c0 + 1, p.nx)};
-  // Local columns 3 .. 3 + kMarchTileX - 1 of the 64 are written.
-  const bool out[2] = {lane >= 2 && lane <= 30 && c0 < p.nx, lane >= 1 && lane <= 29 && c0 + 1 < p.nx};
+  const int c0 = x0 - 3 + NC * lane;  // this lane's columns: c0 .. c0 + NC - 1
+  const int xlast = min(x0 + TX, p.nx) - 1;
+  int gx[NC], cx[NC];
+  bool out[NC];
+#pragma unroll
+  for (int h = 0; h < NC; ++h) {
+    gx[h] = wrap_fast(c0 + h, p.nx);
+    // Local columns 3 .. 32 NC - 4 of the strip are written.
+    const int local = NC * lane + h;
+    out[h] = local >= 3 && local <= 32 * NC - 4 && c0 + h < p.nx;
+    // Column of the RK combine's loads: the lane's own for written cells,
+    // else the nearest written column of the tile (same cache lines, no
+    // divergence).
+    cx[h] = min(max(c0 + h, x0), xlast);
+  }
   const R* __restrict__ U = static_cast<const R*>(p.U);
   const R* __restrict__ V = static_cast<const R*>(p.V);
   R* Uo = static_cast<R*>(p.Uout);
   R* Vo = static_cast<R*>(p.Vout);
-  const R* __restrict__ tau = static_cast<const R*>(p.tau);
+  const R* __restrict__ tau = kLean ? nullptr : static_cast<const R*>(p.tau);
+  const bool visc = !kLean && p.visc_on;
+  const bool drag = !kLean && p.drag_on;
+  const bool blend = kLean ? FORM == kMarchLeanBlend : (bool)p.blend;
   Gas<R> gas;
   gas.cs = k.cs;
   gas.cs2 = k.cs2;
@@ -174,24 +213,26 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   const R ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
   constexpr unsigned kAll = 0xffffffffu;
 
-  MarchColumn<R> col[2];
+  MarchColumn<R> col[NC];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) col[h].W4 = col[h].W3 = col[h].W2 = col[h].W1 = col[h].W0 = col[h].Ay2 =
+  for (int h = 0; h < NC; ++h) col[h].W4 = col[h].W3 = col[h].W2 = col[h].W1 = col[h].W0 = col[h].Ay2 =
       col[h].hy3 = col[h].Fy3 = Cell4<R>{};
   R vmax0 = R(0), vmax1 = R(0);
   const int iters = TY + 6;
-  Cell4<R> next[2];
+  Cell4<R> next[NC];
   {
     const size_t row = (size_t)wrap_fast(y0 - 3, p.ny) * p.nx;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) next[h] = load_cell<R, NV>(U + (row + gx[h]) * NV);
+    for (int h = 0; h < NC; ++h) next[h] = load_cell<R, NV>(U + (row + gx[h]) * NV);
   }
-  for (int it = 0; it < iters; ++it) {
+  // One row of the walk: row j = y0 - 3 + it arrives. STEADY: it >= 6.
+  auto walk_row = [&](const int it, auto steady_tag) {
+    constexpr bool kSteady = decltype(steady_tag)::value;
     const int j = y0 - 3 + it;
-    // ---- y sweep of both columns -------------------------------------------
-    Cell4<R> Ay1[2], lo[2], hi[2], Fy2[2];
+    // ---- y sweep of every column -------------------------------------------
+    Cell4<R> Ay1[NC], lo[NC], hi[NC], Fy2[NC];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < NC; ++h) {
       MarchColumn<R>& c = col[h];
       c.W4 = c.W3;
       c.W3 = c.W2;
@@ -199,112 +240,131 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
       c.W1 = c.W0;
       c.W0 = recover_cell<R, NV>(next[h], k.dfloor);
     }
-    if (it + 1 < iters) {
+    {
+      // The row after this one (past the tile's last row: a wrapped row
+      // that is never used, cheaper than a test).
       const size_t row = (size_t)wrap_fast(j + 1, p.ny) * p.nx;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) next[h] = load_cell<R, NV>(U + (row + gx[h]) * NV);
+      for (int h = 0; h < NC; ++h) next[h] = load_cell<R, NV>(U + (row + gx[h]) * NV);
     }
     // The saved register V is read once, by the RK combine of row j-3; ask L2
     // for row j-1 now (two rows ahead, no registers held) so that the combine
     // does not wait for DRAM. Only cells the combine will read.
-    if (PREFETCH_V && it >= 4 && j - 1 < p.ny && j - 1 < y0 + TY) {
+    if (PREFETCH_V && (kSteady || it >= 4) && j - 1 < p.ny && j - 1 < y0 + TY) {
       const size_t row = (size_t)(j - 1) * p.nx;
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
+      for (int h = 0; h < NC; ++h)
         if (out[h]) asm volatile("prefetch.global.L2 [%0];" ::"l"(V + (row + (size_t)(c0 + h)) * NV));
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < NC; ++h) {
       MarchColumn<R>& c = col[h];
       Ay1[h] = c.Ay2;
-      if (it >= 3 && ReconTraits<RECON>::kFaceShared) Ay1[h] = faces_cells<RECON, R, NV>(c.W3, c.W2, c.W1, c.W0);
+      if ((kSteady || it >= 3) && ReconTraits<RECON>::kFaceShared) Ay1[h] = faces_cells<RECON, R, NV>(c.W3, c.W2, c.W1, c.W0);
       hi[h] = c.hy3;
       lo[h] = c.hy3;
-      if (it >= 4) edges_cells<RECON, R, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1[h], k.dfloor, lo[h], hi[h]);
+      if (kSteady || it >= 4) edges_cells<RECON, R, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1[h], k.dfloor, lo[h], hi[h]);
       Fy2[h] = c.Fy3;
     }
-    if (it >= 5) {
+    if (kSteady || it >= 5) {
       // Faces between rows j-3 (a) and j-2 (b).
 #pragma unroll
-      for (int h = 0; h < 2; ++h) Fy2[h] = face_flux_cells<RS, 1, R, NV>(col[h].hy3, lo[h], gas);
-      if (p.visc_on) {
-        // Transverse x differences: columns c-1 and c+1 of rows j-3 and j-2.
-        const R lbx = __shfl_up_sync(kAll, col[1].W2.v[1], 1), lax = __shfl_up_sync(kAll, col[1].W3.v[1], 1);
-        const R lby = __shfl_up_sync(kAll, col[1].W2.v[2], 1), lay = __shfl_up_sync(kAll, col[1].W3.v[2], 1);
-        const R rbx = __shfl_down_sync(kAll, col[0].W2.v[1], 1), rax = __shfl_down_sync(kAll, col[0].W3.v[1], 1);
-        const R rby = __shfl_down_sync(kAll, col[0].W2.v[2], 1), ray = __shfl_down_sync(kAll, col[0].W3.v[2], 1);
-        // column c0: c0-1 from the left lane, c0+1 = own second column
-        viscous_add<1, R>(p, k, col[0].W3.v[0], col[0].W2.v[0], col[0].W3.v[1], col[0].W3.v[2], col[0].W2.v[1],
-                          col[0].W2.v[2], col[1].W2.v[1] + col[1].W3.v[1], col[1].W2.v[2] + col[1].W3.v[2],
-                          lbx + lax, lby + lay, Fy2[0]);
-        // column c0+1: c0 = own first column, c0+2 from the right lane
-        viscous_add<1, R>(p, k, col[1].W3.v[0], col[1].W2.v[0], col[1].W3.v[1], col[1].W3.v[2], col[1].W2.v[1],
-                          col[1].W2.v[2], rbx + rax, rby + ray, col[0].W2.v[1] + col[0].W3.v[1],
-                          col[0].W2.v[2] + col[0].W3.v[2], Fy2[1]);
+      for (int h = 0; h < NC; ++h) Fy2[h] = face_flux_cells<RS, 1, R, NV>(col[h].hy3, lo[h], gas);
+      if (visc) {
+        // Transverse x differences: (row j-2 + row j-3) at columns h+1 and h-1.
+        R sx[NC + 2], sy[NC + 2];  // sx[h + 1]: column h, h = -1 .. NC
+#pragma unroll
+        for (int h = 0; h < NC; ++h) {
+          sx[h + 1] = col[h].W2.v[1] + col[h].W3.v[1];
+          sy[h + 1] = col[h].W2.v[2] + col[h].W3.v[2];
+        }
+        // The neighbours' sums are formed from shuffled addends, in the same
+        // order, so every column's sum is the same number.
+        sx[0] = __shfl_up_sync(kAll, col[NC - 1].W2.v[1], 1) + __shfl_up_sync(kAll, col[NC - 1].W3.v[1], 1);
+        sy[0] = __shfl_up_sync(kAll, col[NC - 1].W2.v[2], 1) + __shfl_up_sync(kAll, col[NC - 1].W3.v[2], 1);
+        sx[NC + 1] = __shfl_down_sync(kAll, col[0].W2.v[1], 1) + __shfl_down_sync(kAll, col[0].W3.v[1], 1);
+        sy[NC + 1] = __shfl_down_sync(kAll, col[0].W2.v[2], 1) + __shfl_down_sync(kAll, col[0].W3.v[2], 1);
+#pragma unroll
+        for (int h = 0; h < NC; ++h)
+          viscous_add<1, R>(p, k, col[h].W3.v[0], col[h].W2.v[0], col[h].W3.v[1], col[h].W3.v[2], col[h].W2.v[1],
+                            col[h].W2.v[2], sx[h + 2], sy[h + 2], sx[h], sy[h], Fy2[h]);
       }
       if (tau) {
         const size_t rb = (size_t)wrap_fast(j - 2, p.ny) * p.nx, ra = (size_t)wrap_fast(j - 3, p.ny) * p.nx;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < NC; ++h) {
           const R* tb = tau + (rb + gx[h]) * 3;
           const R* ta = tau + (ra + gx[h]) * 3;
-          Fy2[h].v[1] = Fy2[h].v[1] + R(0.5) * (ta[1] + tb[1]);
-          Fy2[h].v[2] = Fy2[h].v[2] + R(0.5) * (ta[2] + tb[2]);
+          Fy2[h].v[1] = add_half_sum(Fy2[h].v[1], ta[1], tb[1]);
+          Fy2[h].v[2] = add_half_sum(Fy2[h].v[2], ta[2], tb[2]);
         }
       }
     }
-    if (it >= 6) {
+    if (kSteady) {
       // ---- x sweep of row r = j-3 across the lanes -------------------------
       const int r = j - 3;
-      const Cell4<R>& a = col[0].W3;
-      const Cell4<R>& b = col[1].W3;
-      const Cell4<R> La = shfl_up_cell<R, NV>(a, 1), Lb = shfl_up_cell<R, NV>(b, 1);
-      const Cell4<R> Ra = shfl_down_cell<R, NV>(a, 1), Rb = shfl_down_cell<R, NV>(b, 1);
-      Cell4<R> A0 = a, A1 = a, A2 = a;
+      Cell4<R> own[NC];
+#pragma unroll
+      for (int h = 0; h < NC; ++h) own[h] = col[h].W3;
+      Cell4<R> E[NC + 4];  // E[k + 2]: column c0 + k
+      lane_cells<NC, R, NV>(own, E);
+      Cell4<R> A[NC + 1];  // A[h]: face between columns h-1 and h
+#pragma unroll
+      for (int h = 0; h <= NC; ++h) A[h] = E[2];
       if constexpr (ReconTraits<RECON>::kFaceShared) {
-        A0 = faces_cells<RECON, R, NV>(La, Lb, a, b);  // face c0 (between c0-1 and c0)
-        A1 = faces_cells<RECON, R, NV>(Lb, a, b, Ra);  // face c0+1
-        A2 = shfl_down_cell<R, NV>(A0, 1);             // face c0+2
+#pragma unroll
+        for (int h = 0; h < NC; ++h) A[h] = faces_cells<RECON, R, NV>(E[h], E[h + 1], E[h + 2], E[h + 3]);
+        A[NC] = shfl_down_cell<R, NV>(A[0], 1);
       }
-      Cell4<R> lo0, hi0, lo1, hi1;
-      edges_cells<RECON, R, NV>(La, Lb, a, b, Ra, A0, A1, k.dfloor, lo0, hi0);
-      edges_cells<RECON, R, NV>(Lb, a, b, Ra, Rb, A1, A2, k.dfloor, lo1, hi1);
-      const Cell4<R> hiL = shfl_up_cell<R, NV>(hi1, 1);  // upper edge of column c0-1
-      Cell4<R> F0 = face_flux_cells<RS, 0, R, NV>(hiL, lo0, gas);  // face c0
-      Cell4<R> F1 = face_flux_cells<RS, 0, R, NV>(hi0, lo1, gas);  // face c0+1
-      if (p.visc_on) {
+      Cell4<R> lx[NC], hx[NC];
+#pragma unroll
+      for (int h = 0; h < NC; ++h)
+        edges_cells<RECON, R, NV>(E[h], E[h + 1], E[h + 2], E[h + 3], E[h + 4], A[h], A[h + 1], k.dfloor, lx[h], hx[h]);
+      const Cell4<R> hiL = shfl_up_cell<R, NV>(hx[NC - 1], 1);  // upper edge of column c0-1
+      Cell4<R> F[NC + 1];  // F[h]: flux at face h
+#pragma unroll
+      for (int h = 0; h < NC; ++h) F[h] = face_flux_cells<RS, 0, R, NV>(h == 0 ? hiL : hx[h - 1], lx[h], gas);
+      if (visc) {
         // Transverse y differences: rows r+1 (W2) and r-1 (W4) at the face's two columns.
-        const Cell4<R>& u0 = col[0].W2;
-        const Cell4<R>& u1 = col[1].W2;
-        const Cell4<R>& d0 = col[0].W4;
-        const Cell4<R>& d1 = col[1].W4;
-        const R lux = __shfl_up_sync(kAll, u1.v[1], 1), luy = __shfl_up_sync(kAll, u1.v[2], 1);
-        const R ldx = __shfl_up_sync(kAll, d1.v[1], 1), ldy = __shfl_up_sync(kAll, d1.v[2], 1);
-        viscous_add<0, R>(p, k, Lb.v[0], a.v[0], Lb.v[1], Lb.v[2], a.v[1], a.v[2], u0.v[1] + lux, u0.v[2] + luy,
-                          d0.v[1] + ldx, d0.v[2] + ldy, F0);
-        viscous_add<0, R>(p, k, a.v[0], b.v[0], a.v[1], a.v[2], b.v[1], b.v[2], u1.v[1] + u0.v[1],
-                          u1.v[2] + u0.v[2], d1.v[1] + d0.v[1], d1.v[2] + d0.v[2], F1);
+        R ux[NC + 1], uy[NC + 1], dx[NC + 1], dy[NC + 1];  // [h + 1]: column h, h = -1 .. NC-1
+#pragma unroll
+        for (int h = 0; h < NC; ++h) {
+          ux[h + 1] = col[h].W2.v[1];
+          uy[h + 1] = col[h].W2.v[2];
+          dx[h + 1] = col[h].W4.v[1];
+          dy[h + 1] = col[h].W4.v[2];
+        }
+        ux[0] = __shfl_up_sync(kAll, col[NC - 1].W2.v[1], 1);
+        uy[0] = __shfl_up_sync(kAll, col[NC - 1].W2.v[2], 1);
+        dx[0] = __shfl_up_sync(kAll, col[NC - 1].W4.v[1], 1);
+        dy[0] = __shfl_up_sync(kAll, col[NC - 1].W4.v[2], 1);
+#pragma unroll
+        for (int h = 0; h < NC; ++h) {
+          const Cell4<R>& a = E[h + 1];  // column h-1
+          const Cell4<R>& b = E[h + 2];  // column h
+          viscous_add<0, R>(p, k, a.v[0], b.v[0], a.v[1], a.v[2], b.v[1], b.v[2], ux[h + 1] + ux[h], uy[h + 1] + uy[h],
+                            dx[h + 1] + dx[h], dy[h + 1] + dy[h], F[h]);
+        }
       }
       if (tau) {
         const size_t rr = (size_t)wrap_fast(r, p.ny) * p.nx;
         const int gm = wrap_fast(c0 - 1, p.nx);
-        const R* t0 = tau + (rr + gx[0]) * 3;
-        const R* t1 = tau + (rr + gx[1]) * 3;
-        const R* tm = tau + (rr + gm) * 3;
-        F0.v[1] = F0.v[1] + R(0.5) * (tm[0] + t0[0]);
-        F0.v[2] = F0.v[2] + R(0.5) * (tm[1] + t0[1]);
-        F1.v[1] = F1.v[1] + R(0.5) * (t0[0] + t1[0]);
-        F1.v[2] = F1.v[2] + R(0.5) * (t0[1] + t1[1]);
+#pragma unroll
+        for (int h = 0; h < NC; ++h) {
+          const R* ta = tau + (rr + (h == 0 ? gm : gx[h - 1])) * 3;
+          const R* tb = tau + (rr + gx[h]) * 3;
+          F[h].v[1] = add_half_sum(F[h].v[1], ta[0], tb[0]);
+          F[h].v[2] = add_half_sum(F[h].v[2], ta[1], tb[1]);
+        }
       }
-      const Cell4<R> F2 = shfl_down_cell<R, NV>(F0, 1);  // face c0+2
+      F[NC] = shfl_down_cell<R, NV>(F[0], 1);  // face c0 + NC
       if (r < p.ny) {
         const size_t row = (size_t)r * p.nx;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (!out[h]) continue;
-          const size_t cell = row + (size_t)(c0 + h);
-          const Cell4<R>& fl = h == 0 ? F0 : F1;
-          const Cell4<R>& fr = h == 0 ? F1 : F2;
+        for (int h = 0; h < NC; ++h) {
+          const size_t cell = row + (size_t)cx[h];
+          const Cell4<R>& fl = F[h];
+          const Cell4<R>& fr = F[h + 1];
           const Cell4<R>& w = col[h].W3;
           Cell4<R> u = load_cell<R, NV>(U + cell * NV);
           u.v[0] = w.v[0];  // the floored density
@@ -313,33 +373,44 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
           Cell4<R> un;
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
-            if (p.has_delta) vs.v[v] = vs.v[v] + k.delta * u.v[v];
-            un.v[v] = rk_combine<R>(p.blend, k.g0, k.g1, u.v[v], vs.v[v], fr.v[v] - fl.v[v],
-                                    Fy2[h].v[v] - col[h].Fy3.v[v], ncx, ncy);
+            if (p.has_delta) vs.v[v] = delta_update(vs.v[v], k.delta, u.v[v]);
+            // The flux differences round on their own: a flux held in this
+            // thread's registers (not read back from another lane) must not be
+            // fused into the difference.
+            un.v[v] = rk_combine<R>(blend, k.g0, k.g1, u.v[v], vs.v[v], Ops<R>::sub(fr.v[v], fl.v[v]),
+                                    Ops<R>::sub(Fy2[h].v[v], col[h].Fy3.v[v]), ncx, ncy);
           }
           un.v[3] = NV == 4 ? un.v[3] : R(0);
-          if (p.drag_on) {
-            un.v[1] = un.v[1] + -((kdrag * w.v[0]) * w.v[1]);
-            un.v[2] = un.v[2] + -((kdrag * w.v[0]) * w.v[2]);
+          if (drag) {
+            un.v[1] = drag_term(un.v[1], kdrag * w.v[0], w.v[1]);
+            un.v[2] = drag_term(un.v[2], kdrag * w.v[0], w.v[2]);
           }
-          if (p.has_delta && Vo) store_cell<R, NV>(Vo + cell * NV, vs);
           if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
-          store_cell<R, NV>(Uo + cell * NV, un);
+          if (out[h]) {
+            if (p.has_delta && Vo) store_cell<R, NV>(Vo + cell * NV, vs);
+            store_cell<R, NV>(Uo + cell * NV, un);
+          }
           if (p.want_cfl) {
             const R inv = Num<R>::rcp(un.v[0]);
-            vmax0 = N::nanmax_pos(vmax0, fabs(inv * un.v[1]) + k.cs);
-            vmax1 = N::nanmax_pos(vmax1, fabs(inv * un.v[2]) + k.cs);
+            const R s0 = signal_speed(inv, un.v[1], k.cs), s1 = signal_speed(inv, un.v[2], k.cs);
+            if (out[h]) {
+              vmax0 = N::nanmax_pos(vmax0, s0);
+              vmax1 = N::nanmax_pos(vmax1, s1);
+            }
           }
         }
       }
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < NC; ++h) {
       col[h].Ay2 = Ay1[h];
       col[h].hy3 = hi[h];
       col[h].Fy3 = Fy2[h];
     }
-  }
+  };
+  for (int it = 0; it < 6; ++it) walk_row(it, Flag<false>{});
+#pragma unroll 1
+  for (int it = 6; it < iters; ++it) walk_row(it, Flag<true>{});
   if (p.want_cfl) {
     const double m0 = warp_nan_max(static_cast<double>(vmax0));
     const double m1 = warp_nan_max(static_cast<double>(vmax1));
@@ -352,34 +423,45 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   }
 }
 
-// Resident warps per SM the float32 kernels are compiled for, the most whose
-// registers still hold every live value (no spills): for one solve, whose
-// stage parameters sit in the constant bank, 16 (128 registers per thread)
-// with DC/PLM/PPM4 and 12 with the longer PPMX/WENO-Z stencils; the batch
-// kernel holds the parameters in registers and gets 12 and 8. The float64
-// kernels use what they need.
-template <typename R, int RECON> constexpr int march_min_blocks() {
-  return sizeof(R) == 4 ? (RECON >= 3 ? 12 : 16) / kMarchWarps : 1;
+// The form a stage runs in (see MarchForm).
+__host__ __device__ inline int march_form(const StageParams& p) {
+  if (p.visc_on || p.tau || p.drag_on) return kMarchGeneric;
+  return p.blend ? kMarchLeanBlend : kMarchLeanPlain;
 }
-template <typename R, int RECON> constexpr int march_batch_min_blocks() {
-  return sizeof(R) == 4 ? (RECON >= 3 ? 8 : 12) / kMarchWarps : 1;
+
+// Resident warps per SM the kernels are compiled for (the register cap),
+// chosen so that every live value stays in registers (no spills): for one
+// float32 solve, whose stage parameters sit in the constant bank, 16 warps
+// (128 registers per thread) with two columns per lane and DC/PLM/PPM4, 12
+// with the longer PPMX/WENO-Z stencils; one column per lane needs fewer
+// registers (24 / 16 warps), three need more (12 / 8). The batch kernel holds
+// the parameters in registers and gets 4 warps fewer. Float64 uses what it
+// needs.
+template <typename R, int RECON, int NC> constexpr int march_min_blocks() {
+  if constexpr (sizeof(R) != 4) return 1;
+  const int two = RECON >= 3 ? 12 : 16;
+  return (NC == 1 ? two + (RECON >= 3 ? 4 : 8) : (NC == 3 ? two - 4 : two)) / kMarchWarps;
+}
+template <typename R, int RECON, int NC> constexpr int march_batch_min_blocks() {
+  return sizeof(R) == 4 ? march_min_blocks<R, RECON, NC>() - 4 / kMarchWarps : 1;
 }
 
 // One warp per tile; the block's warps take consecutive tiles.
-template <typename R, int RECON, int RS, int NV>
-__global__ void __launch_bounds__(kMarchWarps * 32, march_min_blocks<R, RECON>())
+template <typename R, int RECON, int RS, int NV, int NC, int FORM>
+__global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, NC>()))
     stage_kernel_march(const StageParams p, int ntiles) {
   if (p.clock->done) return;
   const int tile = blockIdx.x * kMarchWarps + (threadIdx.x >> 5);
   if (tile >= ntiles) return;
-  march_tile<R, RECON, RS, NV, false>(p, tile, ntiles);
+  march_tile<R, RECON, RS, NV, NC, FORM, false>(p, tile, ntiles);
 }
 
 // Persistent batch kernel over marching tiles (see stage_kernel_batch): each
 // warp takes work items round-robin; nothing is shared between warps. A
-// launch group holds solves of one variable count.
-template <typename R, int RECON, int RS, int NV>
-__global__ void __launch_bounds__(kMarchWarps * 32, march_batch_min_blocks<R, RECON>()) stage_kernel_batch_march(
+// launch group holds solves of one variable count and one column count per
+// lane; each solve's stage options are read at run time.
+template <typename R, int RECON, int RS, int NV, int NC>
+__global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, RECON, NC>())) stage_kernel_batch_march(
     const StageParams* __restrict__ params, const int* __restrict__ tile_offset, int nsolves, int nwork) {
   const int stride = gridDim.x * kMarchWarps;
   for (int w = blockIdx.x * kMarchWarps + (threadIdx.x >> 5); w < nwork; w += stride) {
@@ -392,16 +474,42 @@ __global__ void __launch_bounds__(kMarchWarps * 32, march_batch_min_blocks<R, RE
     const StageParams& p = params[lo];
     if (p.skip || p.clock->done) continue;
     const int tile = w - tile_offset[lo];
-    march_tile<R, RECON, RS, NV, true>(p, tile, tile_offset[lo + 1] - tile_offset[lo]);
+    march_tile<R, RECON, RS, NV, NC, kMarchGeneric, true>(p, tile, tile_offset[lo + 1] - tile_offset[lo]);
   }
 }
 
-// grid.x = number of tiles (one warp each).
+// Float32 stages run in their lean form when they have one; float64 (used
+// only on request: its default is the shared-memory tile) always runs the
+// generic form with two columns per lane. One column per lane (a latency
+// choice for small grids) runs the generic form.
+template <typename R, int RECON, int RS, int NV, int NC>
+cudaError_t launch_march_nc(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4 && NC > 1) {
+    const int form = march_form(p);
+    if (form == kMarchLeanBlend) {
+      stage_kernel_march<R, RECON, RS, NV, NC, kMarchLeanBlend><<<blocks, threads, 0, s>>>(p, ntiles);
+      return cudaGetLastError();
+    }
+    if (form == kMarchLeanPlain) {
+      stage_kernel_march<R, RECON, RS, NV, NC, kMarchLeanPlain><<<blocks, threads, 0, s>>>(p, ntiles);
+      return cudaGetLastError();
+    }
+  }
+  stage_kernel_march<R, RECON, RS, NV, NC, kMarchGeneric><<<blocks, threads, 0, s>>>(p, ntiles);
+  return cudaGetLastError();
+}
+
+// grid.x = number of tiles (one warp each); p.nc selects the columns per lane.
 template <typename R, int RECON, int RS, int NV>
 cudaError_t launch_march_one(const StageParams& p, dim3 grid, cudaStream_t s) {
   const int ntiles = (int)grid.x;
-  stage_kernel_march<R, RECON, RS, NV><<<(ntiles + kMarchWarps - 1) / kMarchWarps, kMarchWarps * 32, 0, s>>>(p, ntiles);
-  return cudaGetLastError();
+  const dim3 blocks((ntiles + kMarchWarps - 1) / kMarchWarps), threads(kMarchWarps * 32);
+  if constexpr (sizeof(R) == 4) {
+    if (p.nc == 1) return launch_march_nc<R, RECON, RS, NV, 1>(p, blocks, threads, ntiles, s);
+    if (p.nc == 3) return launch_march_nc<R, RECON, RS, NV, 3>(p, blocks, threads, ntiles, s);
+  }
+  if (p.nc != 2) return cudaErrorInvalidValue;
+  return launch_march_nc<R, RECON, RS, NV, 2>(p, blocks, threads, ntiles, s);
 }
 
 template <typename R, int RECON>
@@ -415,24 +523,35 @@ cudaError_t launch_march_typed(int rsolver, const StageParams& p, dim3 grid, cud
   return cudaErrorInvalidValue;
 }
 
-template <typename R, int RECON, int NV>
-cudaError_t launch_batch_march_nv(int rsolver, const StageParams* params, const int* offsets, int nsolves,
-                                  int nwork, dim3 grid, cudaStream_t s) {
+template <typename R, int RECON, int NV, int NC>
+cudaError_t launch_batch_march_nc(int rsolver, const StageParams* params, const int* offsets, int nsolves, int nwork,
+                                  dim3 grid, cudaStream_t s) {
   constexpr int T = kMarchWarps * 32;
   switch (rsolver) {
-    case JX_LLF: stage_kernel_batch_march<R, RECON, JX_LLF, NV><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
-    case JX_HLLE: stage_kernel_batch_march<R, RECON, JX_HLLE, NV><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
-    case JX_ROE: stage_kernel_batch_march<R, RECON, JX_ROE, NV><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
+    case JX_LLF: stage_kernel_batch_march<R, RECON, JX_LLF, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
+    case JX_HLLE: stage_kernel_batch_march<R, RECON, JX_HLLE, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
+    case JX_ROE: stage_kernel_batch_march<R, RECON, JX_ROE, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
+template <typename R, int RECON, int NV>
+cudaError_t launch_batch_march_nv(int rsolver, int nc, const StageParams* params, const int* offsets, int nsolves,
+                                  int nwork, dim3 grid, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4) {
+    if (nc == 1) return launch_batch_march_nc<R, RECON, NV, 1>(rsolver, params, offsets, nsolves, nwork, grid, s);
+    if (nc == 3) return launch_batch_march_nc<R, RECON, NV, 3>(rsolver, params, offsets, nsolves, nwork, grid, s);
+  }
+  if (nc != 2) return cudaErrorInvalidValue;
+  return launch_batch_march_nc<R, RECON, NV, 2>(rsolver, params, offsets, nsolves, nwork, grid, s);
+}
+
 template <typename R, int RECON>
-cudaError_t launch_batch_march_typed(int rsolver, int nv, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_typed(int rsolver, int nv, int nc, const StageParams* params, const int* offsets,
                                      int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  return nv == 3 ? launch_batch_march_nv<R, RECON, 3>(rsolver, params, offsets, nsolves, nwork, grid, s)
-                 : launch_batch_march_nv<R, RECON, 4>(rsolver, params, offsets, nsolves, nwork, grid, s);
+  return nv == 3 ? launch_batch_march_nv<R, RECON, 3>(rsolver, nc, params, offsets, nsolves, nwork, grid, s)
+                 : launch_batch_march_nv<R, RECON, 4>(rsolver, nc, params, offsets, nsolves, nwork, grid, s);
 }
 
 }  // namespace jx
@@ -446,11 +565,11 @@ cudaError_t launch_march_recon(int dtype, int rsolver, const StageParams& p, dim
 }
 
 template <int RECON>
-cudaError_t launch_batch_march_recon(int dtype, int rsolver, int nv, const StageParams* params, const int* offsets,
-                                     int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+cudaError_t launch_batch_march_recon(int dtype, int rsolver, int nv, int nc, const StageParams* params,
+                                     const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   if (dtype == JX_F64)
-    return launch_batch_march_typed<double, RECON>(rsolver, nv, params, offsets, nsolves, nwork, grid, s);
-  return launch_batch_march_typed<float, RECON>(rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+    return launch_batch_march_typed<double, RECON>(rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+  return launch_batch_march_typed<float, RECON>(rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
 }
 
 template <typename Kernel>
@@ -461,25 +580,34 @@ int march_occupancy(Kernel kernel) {
 }
 
 // Resident marching blocks per SM (single-solve or batch kernel).
-template <typename R, int RECON, int RS>
-int march_blocks_per_sm_rs(int nv, bool batch) {
+template <typename R, int RECON, int RS, int NC>
+int march_blocks_per_sm_nc(int nv, bool batch) {
   if (batch)
-    return nv == 3 ? march_occupancy(stage_kernel_batch_march<R, RECON, RS, 3>)
-                   : march_occupancy(stage_kernel_batch_march<R, RECON, RS, 4>);
-  return nv == 3 ? march_occupancy(stage_kernel_march<R, RECON, RS, 3>)
-                 : march_occupancy(stage_kernel_march<R, RECON, RS, 4>);
+    return nv == 3 ? march_occupancy(stage_kernel_batch_march<R, RECON, RS, 3, NC>)
+                   : march_occupancy(stage_kernel_batch_march<R, RECON, RS, 4, NC>);
+  return nv == 3 ? march_occupancy(stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric>)
+                 : march_occupancy(stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric>);
+}
+
+template <typename R, int RECON, int RS>
+int march_blocks_per_sm_rs(int nv, int nc, bool batch) {
+  if constexpr (sizeof(R) == 4) {
+    if (nc == 1) return march_blocks_per_sm_nc<R, RECON, RS, 1>(nv, batch);
+    if (nc == 3) return march_blocks_per_sm_nc<R, RECON, RS, 3>(nv, batch);
+  }
+  return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, batch) : 0;
 }
 
 template <int RECON>
-int march_blocks_per_sm_recon(int dtype, int rsolver, int nv, bool batch) {
+int march_blocks_per_sm_recon(int dtype, int rsolver, int nv, int nc, bool batch) {
   if (dtype == JX_F64) {
-    if (rsolver == JX_LLF) return march_blocks_per_sm_rs<double, RECON, JX_LLF>(nv, batch);
-    if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<double, RECON, JX_HLLE>(nv, batch);
-    return march_blocks_per_sm_rs<double, RECON, JX_ROE>(nv, batch);
+    if (rsolver == JX_LLF) return march_blocks_per_sm_rs<double, RECON, JX_LLF>(nv, nc, batch);
+    if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<double, RECON, JX_HLLE>(nv, nc, batch);
+    return march_blocks_per_sm_rs<double, RECON, JX_ROE>(nv, nc, batch);
   }
-  if (rsolver == JX_LLF) return march_blocks_per_sm_rs<float, RECON, JX_LLF>(nv, batch);
-  if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<float, RECON, JX_HLLE>(nv, batch);
-  return march_blocks_per_sm_rs<float, RECON, JX_ROE>(nv, batch);
+  if (rsolver == JX_LLF) return march_blocks_per_sm_rs<float, RECON, JX_LLF>(nv, nc, batch);
+  if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<float, RECON, JX_HLLE>(nv, nc, batch);
+  return march_blocks_per_sm_rs<float, RECON, JX_ROE>(nv, nc, batch);
 }
 
 }  // namespace jx

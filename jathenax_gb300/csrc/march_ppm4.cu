@@ -6,11 +6,11 @@ namespace jx {
 cudaError_t launch_march_ppm4(int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
   return launch_march_recon<JX_PPM4>(dtype, rsolver, p, grid, s);
 }
-cudaError_t launch_batch_march_ppm4(int dtype, int rsolver, int nv, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_ppm4(int dtype, int rsolver, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  return launch_batch_march_recon<JX_PPM4>(dtype, rsolver, nv, params, offsets, nsolves, nwork, grid, s);
+  return launch_batch_march_recon<JX_PPM4>(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
 }
-int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, bool batch) {
-  return march_blocks_per_sm_recon<JX_PPM4>(dtype, rsolver, nv, batch);
+int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, bool batch) {
+  return march_blocks_per_sm_recon<JX_PPM4>(dtype, rsolver, nv, nc, batch);
 }
 }  // namespace jx

@@ -8,8 +8,7 @@ identical to the reference's. The device half (``render_force``,
 """
 
 import ctypes
-from fractions import Fraction
-from math import exp, log, pi, sqrt
+from math import log, pi, sqrt
 
 import numpy as np
 
@@ -82,17 +81,14 @@ def cartesian_modes(nlow, nhigh, kx_bounds, ky_bounds):
     return modes
 
 
-def _fused_multiply_add(a, b, c):
-    """Correctly rounded a*b + c (exact rational product, one rounding)."""
-    return float(Fraction(a) * Fraction(b) + Fraction(c))
-
-
 def modal_coefficients(modes, lengths, nlow, nhigh, npeak, sol_fraction, rseed,
                        tcorr, dt_update, updates):
     """OU modal table [update, mode, dir, re/im] in float64 (forcing.py:63-100).
 
-    Generated by libjx.so's host routine jx_ou_table, which is bit-identical
-    to :func:`modal_coefficients_python` and much faster for long runs.
+    Generated by libjx.so's host routine jx_ou_table (C++, integer LCG draws
+    and IEEE float64 operations in the reference's order, so the table is
+    bitwise the reference's; the tests pin it against the reference's own
+    output).
     """
     if not nlow <= npeak <= nhigh or not 0.0 <= sol_fraction <= 1.0:
         raise ValueError("npeak must be in the forcing band and sol_fraction in [0, 1]")
@@ -106,43 +102,6 @@ def modal_coefficients(modes, lengths, nlow, nhigh, npeak, sol_fraction, rseed,
         float(dt_update), int(updates), out.ctypes.data_as(ctypes.c_void_p))
     if status != 0:
         raise ValueError("invalid forcing table arguments")
-    return out
-
-
-def modal_coefficients_python(modes, lengths, nlow, nhigh, npeak, sol_fraction, rseed,
-                              tcorr, dt_update, updates):
-    """Pure-Python OU table, the step-by-step restatement of forcing.py:63-100."""
-    if not nlow <= npeak <= nhigh or not 0.0 <= sol_fraction <= 1.0:
-        raise ValueError("npeak must be in the forcing band and sol_fraction in [0, 1]")
-    if not np.isfinite(tcorr) or tcorr < 0.0 or not 0.0 < dt_update < np.inf:
-        raise ValueError("tcorr must be finite and nonnegative and dt_update positive")
-    modes = np.asarray(modes)
-    dk = 2.0 * pi / np.asarray(lengths)
-    k = modes * dk
-    kabs = np.sqrt(k[:, 0]**2 + k[:, 1]**2)
-    kpeak = npeak * 2.0 * pi / lengths[0]
-    band = nhigh * max(dk) - nlow * min(dk)
-    slope = float(-4.0 / band**2)
-    # Parabolic spectrum evaluated with one rounding, as AthenaK's compiler
-    # contracts it into an FMA (matters at the band edge).
-    spectrum = np.array([_fused_multiply_add(slope, float(d2), 1.0) for d2 in (kabs - kpeak)**2])
-    weight = np.sqrt(np.abs(spectrum))
-    weight *= np.sqrt(kpeak / kabs)
-
-    decay = exp(-dt_update / tcorr) if tcorr > 1e-6 else 0.0
-    refresh = sqrt(1.0 - decay * decay)
-    draws = ran_gaussian_st(rseed)
-    count = 4 * len(modes)
-    out = np.empty((updates, len(modes), 2, 2))
-    k_col = k[:, :, None]
-    kabs2 = kabs[:, None, None]**2
-    for u in range(updates):
-        noise = np.fromiter(draws, dtype=float, count=count).reshape(-1, 2, 2)
-        noise *= weight[:, None, None]
-        k_dot = k[:, 0, None] * noise[:, 0] + k[:, 1, None] * noise[:, 1]
-        longitudinal = k_col * k_dot[:, None] / kabs2
-        noise = sol_fraction * (noise - longitudinal) + (1.0 - sol_fraction) * longitudinal
-        out[u] = noise if u == 0 else decay * out[u - 1] + refresh * noise
     return out
 
 

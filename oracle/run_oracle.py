@@ -13,13 +13,13 @@ from .forcing_oracle import select_update
 from .hydro_oracle import primitives, step, timestep
 
 
-def evolve(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *, nu=0.0, cs_smag=0.0,
-           drag=0.0, forcing=None, dt_update=1.0, t_start=0.0, dedt=0.0, recon="ppm4",
-           solver="roe", stress=None, stress_args=None):
-    """Advance to ``tlim`` or ``nlim`` cycles; returns (U, time, dt, cycle). run.py:20-69.
+def evolve_iter(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *, nu=0.0, cs_smag=0.0,
+                drag=0.0, forcing=None, dt_update=1.0, t_start=0.0, dedt=0.0, recon="ppm4",
+                solver="roe", stress=None, stress_args=None):
+    """The loop of ``evolve`` yielding (U, time, dt, cycle) after every cycle; run.py:20-69.
 
-    ``forcing`` is ``(table, phase_tables)``. Time and dt are kept in U's dtype,
-    as the reference does.
+    Reading the state between cycles does not change the run: the sequence of
+    yielded states is the trajectory ``evolve`` follows to ``tlim``/``nlim``.
     """
     for name, value in (("viscosity", nu), ("smagorinsky_cs", cs_smag),
                         ("drag_rate", drag), ("dedt", dedt)):
@@ -48,7 +48,19 @@ def evolve(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, *, nu=0.0, cs_sma
         time = np.asarray(time + dt, dtype=dtype)
         prev = dt
         cycle += 1
-    return U, time, prev, cycle
+        yield U, time, prev, cycle
+
+
+def evolve(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, **kw):
+    """Advance to ``tlim`` or ``nlim`` cycles; returns (U, time, dt, cycle). run.py:20-69.
+
+    Keywords as :func:`evolve_iter` (``forcing`` is ``(table, phase_tables)``).
+    Time and dt are kept in U's dtype, as the reference does.
+    """
+    out = (U, np.asarray(0.0, dtype=U.dtype), np.asarray(np.inf, dtype=U.dtype), 0)
+    for out in evolve_iter(U, dx, dy, cs, dfloor, integrator, cfl, tlim, nlim, **kw):
+        pass
+    return out
 
 
 def cell_centers(nx, ny):

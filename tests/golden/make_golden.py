@@ -2,7 +2,7 @@
 
 Usage (needs the reference source tree, e.g. a checkout of JathenAX):
 
-    python tests/golden/make_golden.py --reference /root/reference
+    python tests/golden/make_golden.py --reference <path-to-JathenAX-checkout>
 
 JathenAX needs jax/jaxlib, which are not installable here, so the reference's
 unmodified package is imported on top of ``oracle/jaxshim`` (a NumPy-backed

@@ -79,6 +79,14 @@ def test_workspace_and_tiles():
     assert (tx.value, ty.value) == (32, 16) and smem.value <= 112 * 1024
     assert lib.jx_tile_info(ctypes.byref(_desc(nvar=3, tile_x=58, tile_y=4)), ctypes.byref(tx),
                             ctypes.byref(ty), ctypes.byref(smem)) == _lib.JX_ERR_INVALID
+    # 26- and 90-column tiles: the marching kernel with one and three columns
+    # per lane (float32); float64 marches with two columns only.
+    for width in (26, 90):
+        assert lib.jx_tile_info(ctypes.byref(_desc(nvar=4, dtype=_lib.JX_F32, tile_x=width, tile_y=12)),
+                                ctypes.byref(tx), ctypes.byref(ty), ctypes.byref(smem)) == 0
+        assert (tx.value, ty.value, smem.value) == (width, 12, 0)
+        assert lib.jx_tile_info(ctypes.byref(_desc(nvar=4, tile_x=width, tile_y=12)), ctypes.byref(tx),
+                                ctypes.byref(ty), ctypes.byref(smem)) == _lib.JX_ERR_INVALID
     # Many scalars shrink the default tile to keep two CTAs per SM.
     assert lib.jx_tile_info(ctypes.byref(_desc(nvar=12)), ctypes.byref(tx), ctypes.byref(ty),
                             ctypes.byref(smem)) == 0

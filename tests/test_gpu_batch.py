@@ -118,3 +118,25 @@ def test_batched_forcing_matches_solo_bitwise():
         alone.run(steps_per_sync=4)
         assert s.state().cycle == alone.state().cycle > 2, spec
         np.testing.assert_array_equal(s.S.cpu().numpy(), alone.S.cpu().numpy(), err_msg=str(spec))
+
+
+def test_float32_batch_mixing_methods_and_columns_per_lane_is_bitwise():
+    """Float32 solves of every reconstruction family in one batch, on marching
+    tiles of 1, 2 and 3 columns per lane and on the shared-memory tile: each
+    is bitwise its own solo run (and the solo runs agree across tiles)."""
+    from jathenax_gb300.batch import Batch, ClockBank
+    specs = [("kh", 40, "float32", "dc", "llf", "rk2", 0.03), ("kh", 52, "float32", "wenoz", "hlle", "rk3", 0.02),
+             ("smooth", 44, "float32", "ppmx", "roe", "rk4", 0.02), ("turb", 36, "float32", "plm", "hlle", "rk3", 0.03)]
+    tiles = [(26, 8), (58, 12), (90, 8), (32, 16)]
+    bank = ClockBank(len(specs) * len(tiles))
+    solves, expect = [], []
+    for i, spec in enumerate(specs):
+        for j, (tx, ty) in enumerate(tiles):
+            solves.append(make_solve(*spec, tile_y=ty, tile_x=tx, clock=bank.slot(i * len(tiles) + j)))
+        expect.append(run_alone(spec, 16, 58))
+    Batch(solves, clocks=bank).run(steps_per_sync=4)
+    for k, s in enumerate(solves):
+        U_alone, t_alone, cyc_alone = expect[k // len(tiles)]
+        c = s.state()
+        assert (c.time, c.cycle) == (t_alone, cyc_alone), (k, c.time, t_alone)
+        np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=f"solve {k}")

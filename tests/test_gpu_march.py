@@ -1,5 +1,6 @@
 """The register-marching stage kernel (58-column tiles) against the
-shared-memory tile kernel (32-column tiles) and the float64 oracle.
+shared-memory tile kernel (32-column tiles) and the float64 oracle; one and
+three columns per lane (26- and 90-column tiles) against two.
 
 Both kernels evaluate every face and cell with the same device functions in
 the same order; where they can still differ is the compiler's contraction of
@@ -11,7 +12,7 @@ magnitude pointwise), over every
 reconstruction and Riemann solver, the viscous, drag and SGS-stress terms,
 RK4's saved-register stages and ragged and tiny periodic grids (fewer cells
 than one strip or one tile); the marching kernel against itself is bitwise
-for every tile height.
+for every tile height and every column count per lane.
 """
 
 import numpy as np
@@ -120,3 +121,56 @@ def test_marching_tile_height_does_not_change_results():
         assert_bitwise(stepped(U0, torch.float32, (58, rows), steps=3), base, f"rows {rows}")
     # The automatic tile (device-dependent height) gives the same state too.
     assert_bitwise(stepped(U0, torch.float32, (0, 0), steps=3), base, "automatic tile")
+
+
+@pytest.mark.parametrize("rs", SOLVERS)
+@pytest.mark.parametrize("rec", RECONS)
+def test_columns_per_lane_do_not_change_results(rec, rs):
+    """Float32, lean (inviscid) forms: 1, 2 and 3 columns per lane, bitwise."""
+    import torch
+    U0 = noisy_state(187, 70, nvar=4, seed=RECONS.index(rec) * 3 + SOLVERS.index(rs) + 40)
+    base = stepped(U0, torch.float32, (58, 16), recon=rec, rsolver=rs, steps=2)
+    for tile in ((26, 16), (90, 12)):
+        assert_bitwise(stepped(U0, torch.float32, tile, recon=rec, rsolver=rs, steps=2), base, f"{rec}/{rs} {tile}")
+
+
+@pytest.mark.parametrize("integrator", ["rk2", "rk4"])
+def test_columns_per_lane_viscous_drag_and_stress(integrator):
+    """Float32, generic form (viscosity, Smagorinsky, drag, SGS stress, RK4's
+    saved register), ragged grid: 1, 2 and 3 columns per lane, bitwise."""
+    import torch
+    U0 = noisy_state(131, 45, nvar=3, seed=9)
+    kw = dict(viscosity=2e-3, smagorinsky_cs=0.2, drag_rate=0.3)
+    tau = 1e-3 * np.random.default_rng(5).standard_normal((45, 131, 3))
+    base = stepped(U0, torch.float32, (58, 12), integrator=integrator, rsolver="hlle", tau=tau, **kw)
+    for tile in ((26, 8), (90, 20)):
+        got = stepped(U0, torch.float32, tile, integrator=integrator, rsolver="hlle", tau=tau, **kw)
+        assert_bitwise(got, base, f"{integrator} {tile}")
+
+
+@pytest.mark.parametrize("shape", [(5, 7), (1, 40), (9, 27), (9, 91), (70, 26), (64, 181)])
+def test_columns_per_lane_on_tiny_and_ragged_grids(shape):
+    import torch
+    ny, nx = shape
+    U0 = noisy_state(nx, ny, nvar=4, seed=ny * nx)
+    for rec in ("ppm4", "wenoz"):
+        base = stepped(U0, torch.float32, (58, 8), recon=rec)
+        for tile in ((26, 8), (90, 8)):
+            assert_bitwise(stepped(U0, torch.float32, tile, recon=rec), base, f"{shape} {rec} {tile}")
+
+
+@pytest.mark.parametrize("rs", SOLVERS)
+@pytest.mark.parametrize("rec", RECONS)
+def test_float32_kernel_families_are_bitwise_equal(rec, rs):
+    """Float32 rounds every operation explicitly, so the shared-memory tile
+    kernel and the marching kernel give the same bits (float64 agrees to the
+    step tolerance only; see test_marching_matches_tile_kernel)."""
+    import torch
+    U0 = noisy_state(150, 66, nvar=4, seed=RECONS.index(rec) * 3 + SOLVERS.index(rs) + 70)
+    a = stepped(U0, torch.float32, (58, 16), recon=rec, rsolver=rs, steps=2)
+    b = stepped(U0, torch.float32, (32, 16), recon=rec, rsolver=rs, steps=2)
+    assert_bitwise(a, b, f"{rec}/{rs}")
+    kw = dict(viscosity=2e-3, smagorinsky_cs=0.2, drag_rate=0.3)
+    a = stepped(U0[..., :3], torch.float32, (26, 12), recon=rec, rsolver=rs, integrator="rk4", **kw)
+    b = stepped(U0[..., :3], torch.float32, (32, 8), recon=rec, rsolver=rs, integrator="rk4", **kw)
+    assert_bitwise(a, b, f"{rec}/{rs} viscous rk4")
