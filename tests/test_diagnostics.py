@@ -67,3 +67,17 @@ def test_diagnostics_command_writes_spectra_csv_and_fields(tmp_path):
     np.testing.assert_allclose(table[:, 1], energy, rtol=1e-15)
     with np.load(tmp_path / "run_fields.npz") as f:
         assert {"final_density", "final_vorticity", "initial_vorticity"} <= set(f.files)
+
+
+def test_shell_spectra_match_the_reference_script(golden):
+    """The reference's own jathenax/spectra.py, run unmodified on these states
+    (tests/golden/make_spectra.py), wrote the fixture's spectra; even, odd and
+    unequal axes exercise the shell binning and the Nyquist derivative."""
+    g = golden("spectra")
+    names = sorted(k[:-2] for k in g if k.endswith("_U"))
+    assert len(names) == 5
+    for name in names:
+        modes, energy, enstrophy = shell_spectra(g[f"{name}_U"])
+        np.testing.assert_array_equal(modes, g[f"{name}_mode"], err_msg=name)
+        np.testing.assert_allclose(energy, g[f"{name}_energy"], rtol=1e-14, atol=0, err_msg=name)
+        np.testing.assert_allclose(enstrophy, g[f"{name}_enstrophy"], rtol=1e-14, atol=1e-300, err_msg=name)
