@@ -72,6 +72,16 @@ def parse_args():
                    help="instead of the benchmark line: time --steps batched cycles (after --warmup) of "
                         "the 64-solve float32 ensemble (or its KH / turbulence half) at --tile")
     p.add_argument("--tile", default="58x32", help="tile of --ensemble, e.g. 58x32 or 32x16")
+    p.add_argument("--precision-sweep", action="store_true",
+                   help="instead of the benchmark line: float32 against float64 L1 density error of every "
+                        "problem x reconstruction x Riemann solver on small served grids (one JSON line each)")
+    p.add_argument("--precision-tlims", default="0.5,1,1.5,2,2.5,3", help="end times of --precision-sweep")
+    p.add_argument("--precision-pairs", default="",
+                   help="problem:reconstruction pairs of --precision-sweep, e.g. kh:ppm4,smooth:wenoz (default all)")
+    p.add_argument("--serve-stated", type=int, default=None, metavar="N",
+                   help="instead of the benchmark line: the stated serving stream (side 64..2048, "
+                        "tlim U[0.2, 3]) with N requests at --serve-rate, against serial float64")
+    p.add_argument("--serve-rate", type=float, default=1000.0)
     p.add_argument("--sweep", action="store_true",
                    help="instead of the benchmark line: one JSON line per reconstruction x Riemann "
                         "solver x integrator x precision on the --n grid (default 1024 here)")
@@ -480,7 +490,7 @@ def bench_batched(torch, tlim=0.05):
     from jathenax_gb300.diagnostics import relative_l1
     from jathenax_gb300.serve import build_solve
     reqs = [make_request(k, n, s, tlim, "float32", i) for i, (k, n, s) in enumerate(ensemble_specs())]
-    tuned = autotune.tune_batch(lambda tile: [build_solve(r, tile) for r in reqs])
+    tuned = autotune.tune_batch([build_solve(r, (0, 0)) for r in reqs])
     bank = ClockBank(len(reqs))
     solves = [build_solve(r, tuned["tile"], clock=bank.slot(i)) for i, r in enumerate(reqs)]
     batch = Batch(solves, blocks_per_sm=tuned["blocks_per_sm"], clocks=bank)
@@ -510,8 +520,11 @@ def bench_batched(torch, tlim=0.05):
             "min_cycles_1024": min(c for c, r in zip(cycles, reqs) if r.side == 1024),
             "cycles_range": [min(cycles), max(cycles)],
             "tile": tuned["tile"], "blocks_per_sm": tuned["blocks_per_sm"],
-            "autotune_ms_per_step": {f"{t['tile'][0]}x{t['tile'][1]}": round(t["ms_per_step"], 3)
-                                     for t in tuned["trials"]},
+            "autotune": {"chosen": tuned["knobs"], "ms_per_step": round(tuned["ms_per_step"], 4),
+                         "knobs": ["staging", "columns_per_lane", "rows", "blocks_per_sm"],
+                         "timing": tuned["timing"], "clock_mhz": tuned["clock_mhz"],
+                         "trials": [[t["staging"], t["columns_per_lane"], t["rows"], t["blocks_per_sm"],
+                                     round(t["ms_per_step"], 4)] for t in tuned["trials"]]},
             "batched_s": round(batched_s, 3), "serial_s": round(serial_s, 3)}
 
 
@@ -540,7 +553,7 @@ def bench_serving(torch, n):
             server.warmup()
             stats = server.run(reqs)
             errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs)
-                    if (dtype or q.dtype) == "float32"]
+                    if q.served_dtype == "float32"]
             # Requests offered per second over the arrival window: a server
             # whose solves/s comes within 20 % of it is bounded by the
             # arrivals, not by its own speed.
@@ -552,10 +565,58 @@ def bench_serving(torch, n):
                 "solves_per_s": round(stats["solves_per_s"], 3),
                 "speedup_vs_serial_fp64": round(stats["solves_per_s"] / serial["solves_per_s"], 2),
                 "tts_p50_s": round(stats["tts_p50_s"], 4), "tts_p99_s": round(stats["tts_p99_s"], 4),
-                "peak_live": stats["peak_live"],
+                "peak_live": stats["peak_live"], "promoted_to_float64": stats["promoted_to_float64"],
                 "fp32_l1_density_err_vs_fp64_max": max(errs) if errs else None,
                 "fp32_l1_density_err_vs_fp64_median": float(np.median(errs)) if errs else None}
+    out["tiles"] = server.tile_table()
     return out
+
+
+def bench_serving_stated(args):
+    """The serving stream as stated: Poisson arrivals, grid side log-uniform in
+    64..2048, problem uniform over smooth/KH/turbulence, random reconstruction and
+    Riemann solver, tlim uniform in [0.2, 3], 80 % float32, 150 GB budget; the
+    first --serve-stated requests of the seeded stream. Serial float64 on the same
+    requests is the baseline and the float64 rerun of every float32 result."""
+    import torch
+    from jathenax_gb300.diagnostics import relative_l1
+    from jathenax_gb300.serve import Server, make_stream, run_serial, warmup_requests
+    torch.cuda.set_device(0)
+    n, rate = args.serve_stated, args.serve_rate
+
+    def stream():
+        return make_stream(n, rate=rate, seed=2026, side_range=(64, 2048), tlim_range=(0.2, 3.0))
+
+    ref = stream()
+    run_serial(warmup_requests(("float64",)), dtype="float64")
+    serial = run_serial(ref, dtype="float64", keep_results=True)
+    out = {"requests": n, "rate": rate, "stream": "Poisson arrivals, side log-uniform 64..2048, tlim U[0.2,3], "
+           "problems smooth/kh/turbulence, random recon/rsolver, 80% float32, 150 GB budget, seed 2026",
+           "sides": [min(r.side for r in ref), int(np.median([r.side for r in ref])), max(r.side for r in ref)],
+           "cell_updates": int(sum(r.side ** 2 * r.cycles for r in ref)),
+           "serial_fp64_s": round(serial["elapsed_s"], 2), "serial_fp64_solves_per_s": round(serial["solves_per_s"], 4)}
+    for label, dtype in (("mixed_80pct_fp32", None), ("all_fp32_unguarded", "float32")):
+        reqs = stream()
+        server = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype,
+                        guard=dtype is None)
+        server.warmup()
+        stats = server.run(reqs)
+        errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs) if q.served_dtype == "float32"]
+        window = max(q.arrival for q in reqs) - min(q.arrival for q in reqs)
+        offered = (len(reqs) - 1) / window if window > 0 else float("inf")
+        out[label] = {"solves_per_s": round(stats["solves_per_s"], 4), "elapsed_s": round(stats["elapsed_s"], 2),
+                      "speedup_vs_serial_fp64": round(stats["solves_per_s"] / serial["solves_per_s"], 2),
+                      "tts_p50_s": round(stats["tts_p50_s"], 3), "tts_p99_s": round(stats["tts_p99_s"], 3),
+                      "offered_per_s": round(offered, 2), "arrival_bound": bool(stats["solves_per_s"] >= 0.8 * offered),
+                      "peak_live": stats["peak_live"], "peak_gb": round(stats["peak_bytes"] / 1e9, 1),
+                      "failed": stats["failed"], "promoted_to_float64": stats["promoted_to_float64"],
+                      "fp32_requests": len(errs),
+                      "fp32_l1_density_err_vs_fp64_max": max(errs) if errs else None,
+                      "fp32_l1_density_err_vs_fp64_median": float(np.median(errs)) if errs else None,
+                      "fp32_over_1e-5": sum(e > 1e-5 for e in errs)}
+        out[f"{label}_tiles"] = server.tile_table()
+        del server
+    print(json.dumps(out), flush=True)
 
 
 def driven_turbulence(side, tlim, dtype, smagorinsky_cs=0.0, seed=1618):
@@ -717,6 +778,43 @@ def bench_reference(args, world, rank):
     }
 
 
+def bench_precision_sweep(args):
+    """Float32 vs float64 L1 density error per (problem, method, side, end time) as served
+    (the serving set-ups, build_solve), one JSON line each: the evidence behind serve.py's
+    float32 precision guard (FP32_TLIM_MAX)."""
+    import torch
+    from jathenax_gb300.diagnostics import relative_l1
+    from jathenax_gb300.serve import PROBLEMS, RECONS, SOLVERS, Request, build_solve
+    torch.cuda.set_device(0)
+    sides = (64, 85, 128, 256) if args.n is None else (args.n,)
+    tlims = tuple(float(t) for t in args.precision_tlims.split(","))
+    pairs = None if not args.precision_pairs else {tuple(p.split(":")) for p in args.precision_pairs.split(",")}
+    for problem in PROBLEMS:
+        for recon in RECONS:
+            if pairs is not None and (problem, recon) not in pairs:
+                continue
+            for rsolver in SOLVERS:
+                for side in sides:
+                    # One run per precision, stopped at each end time in turn (the first
+                    # stop is exactly a request with that end time; each later one
+                    # includes the earlier stops' clipped steps, in both precisions alike).
+                    req = Request(rid=0, arrival=0.0, problem=problem, side=side, reconstruct=recon,
+                                  rsolver=rsolver, tlim=max(tlims), dtype="float32", seed=7)
+                    solves = {dtype: build_solve(req, dtype=dtype) for dtype in ("float32", "float64")}
+                    for tlim in sorted(tlims):
+                        out = {}
+                        for dtype, s in solves.items():
+                            s.set_clock(tlim=tlim, done=0)
+                            s.run(steps_per_sync=64)
+                            out[dtype] = (s.S.cpu().numpy(), s.state())
+                        l1 = relative_l1(out["float32"][0], out["float64"][0])
+                        print(json.dumps({"problem": problem, "method": f"{recon}/{rsolver}", "side": side,
+                                          "tlim": tlim, "l1_density": float(l1[0]), "l1_max": float(np.max(l1)),
+                                          "cycles": [out["float32"][1].cycle, out["float64"][1].cycle]}),
+                              flush=True)
+                    del solves
+
+
 def bench_sweep(args):
     """cell-updates/s of every method combination (graph replays of whole cycles)."""
     import torch
@@ -756,6 +854,12 @@ def main():
     args = parse_args()
     if args.sweep:
         bench_sweep(args)
+        return
+    if args.precision_sweep:
+        bench_precision_sweep(args)
+        return
+    if args.serve_stated:
+        bench_serving_stated(args)
         return
     if args.turbulence_t is not None:
         bench_turbulence_long(args)

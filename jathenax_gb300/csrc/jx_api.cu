@@ -201,7 +201,7 @@ jx_status resolve_tile(const jx_desc* d, Tile* t, bool device = true) {
 }
 
 struct Layout {
-  size_t scal, cfl, p1, p2, box, total;
+  size_t scal, cfl, p1, box, total;
 };
 
 Layout layout_for(const jx_desc* d, const Tile& t) {
@@ -213,10 +213,8 @@ Layout layout_for(const jx_desc* d, const Tile& t) {
   size_t slots = t.cfl_slots;
   if (slots < (size_t)kCflBlocksMax) slots = kCflBlocksMax;
   off = align256(off + slots * kCflSlots * sizeof(double));
-  L.p1 = off;
-  off = align256(off + (size_t)kForceBlocksMax * 4 * sizeof(double));
-  L.p2 = off;
-  off = align256(off + (size_t)kForceBlocksMax * 4 * sizeof(double));
+  L.p1 = off;  // forcing moments, 8 per block
+  off = align256(off + (size_t)kForceBlocksMax * 8 * sizeof(double));
   L.box = off;
   off = align256(off + (size_t)kForceBlocksMax * d->nvar * sizeof(double));
   L.total = off;
@@ -225,7 +223,7 @@ Layout layout_for(const jx_desc* d, const Tile& t) {
 
 struct Ws {
   WsHeader* header;
-  double *scal, *cfl, *p1, *p2, *box;
+  double *scal, *cfl, *p1, *box;
 };
 
 jx_status bind_ws(const jx_desc* d, const Tile& t, void* ws, size_t bytes, Ws* w) {
@@ -238,7 +236,6 @@ jx_status bind_ws(const jx_desc* d, const Tile& t, void* ws, size_t bytes, Ws* w
   w->scal = reinterpret_cast<double*>(b + L.scal);
   w->cfl = reinterpret_cast<double*>(b + L.cfl);
   w->p1 = reinterpret_cast<double*>(b + L.p1);
-  w->p2 = reinterpret_cast<double*>(b + L.p2);
   w->box = reinterpret_cast<double*>(b + L.box);
   return JX_OK;
 }
@@ -400,7 +397,6 @@ ForceParams force_params(const jx_desc* d, const jx_forcing* f, void* U, jx_cloc
   q.Uw = U;
   q.raw = f->raw_force;
   q.p1 = w.p1;
-  q.p2 = w.p2;
   q.scal = w.scal;
   q.partials = w.cfl;
   q.header = w.header;

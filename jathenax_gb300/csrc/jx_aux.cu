@@ -333,89 +333,67 @@ __device__ __forceinline__ void block_grid_sum(GridSum<R> (&a)[K], double (&v)[K
   }
 }
 
-// Pass 1: block partials of sum(rho), sum(rho*Fx), sum(rho*Fy).
+// The normalisation sums of forcing.py:137-149 in one pass. The reference
+// removes the mass-weighted mean mu = sum(rho F) / sum(rho) and then sums
+// 0.5 rho |F - mu|^2 dt and m . (F - mu); expanding the squares gives the
+// same totals from moments that do not need mu:
+//   sum 0.5 rho |F - mu|^2 = Q - 0.5 mu . (A, B),  sum m . (F - mu) = P - mu . M
+// with S = sum rho, (A, B) = sum rho F, Q = sum 0.5 rho |F|^2, M = sum m and
+// P = sum m . F, so one pass over the state (instead of two dependent ones)
+// and one finisher do. The forcing field has no mean of its own (every mode
+// has |k| >= 1), so mu is small and the subtraction loses nothing to
+// cancellation. Block partials: 8 doubles per block (7 used).
 template <typename R>
-__device__ __forceinline__ void sum1_body(const ForceParams& q, int b, double* red) {
+__device__ __forceinline__ void moments_body(const ForceParams& q, int b, double* red) {
   if (q.clock->done) return;
+  using O = Ops<R>;
   const R* U = static_cast<const R*>(q.U);
   const R* F = static_cast<const R*>(q.raw);
   const int64_t n = (int64_t)q.ny * q.nx;
   const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
-  GridSum<R> a[3];
-  for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-    const R rho = U[k * q.nv];
-    a[0].add(rho);
-    a[1].add(rho * F[2 * k]);
-    a[2].add(rho * F[2 * k + 1]);
-  }
-  double v[3];
-  block_grid_sum<3>(a, v, red);
-  if (threadIdx.x == 0) {
-    double* out = q.p1 + (size_t)b * 4;
-    out[0] = v[0];
-    out[1] = v[1];
-    out[2] = v[2];
-  }
-}
-
-// Finish pass 1: the mass-weighted mean acceleration.
-__device__ __forceinline__ void fin1_body(const ForceParams& q, double* red) {
-  if (q.clock->done) return;
-  double v[3] = {0.0, 0.0, 0.0};
-  for (int b = threadIdx.x; b < q.nblk; b += blockDim.x) {
-    v[0] += q.p1[b * 4 + 0];
-    v[1] += q.p1[b * 4 + 1];
-    v[2] += q.p1[b * 4 + 2];
-  }
-  block_sum<3>(v, red);
-  if (threadIdx.x == 0) {
-    q.scal[0] = v[1] / v[0];  // mean_x
-    q.scal[1] = v[2] / v[0];  // mean_y
-  }
-}
-
-// Pass 2: partials of sum(0.5 rho |F - mean|^2 dt) and sum(m . (F - mean)).
-template <typename R>
-__device__ __forceinline__ void sum2_body(const ForceParams& q, int b, double* red) {
-  if (q.clock->done) return;
-  const R* U = static_cast<const R*>(q.U);
-  const R* F = static_cast<const R*>(q.raw);
-  const R mx = static_cast<R>(q.scal[0]), my = static_cast<R>(q.scal[1]);
-  const R dt = static_cast<R>(q.clock->dt);
-  const int64_t n = (int64_t)q.ny * q.nx;
-  const int64_t lo = (int64_t)b * q.chunk, hi = min(n, lo + q.chunk);
-  GridSum<R> a[2];
+  GridSum<R> a[7];
   for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
     const R* u = U + k * q.nv;
-    const R fx = F[2 * k] - mx, fy = F[2 * k + 1] - my;
-    const R f2 = fx * fx + fy * fy;
-    a[0].add(R(0.5) * u[0] * f2 * dt);
-    a[1].add(u[1] * fx + u[2] * fy);
+    const R rho = u[0], mx = u[1], my = u[2];
+    const R fx = F[2 * k], fy = F[2 * k + 1];
+    a[0].add(rho);
+    a[1].add(O::mul(rho, fx));
+    a[2].add(O::mul(rho, fy));
+    a[3].add(O::mul(O::mul(R(0.5), rho), O::fma(fx, fx, O::mul(fy, fy))));
+    a[4].add(mx);
+    a[5].add(my);
+    a[6].add(O::fma(mx, fx, O::mul(my, fy)));
   }
-  double v[2];
-  block_grid_sum<2>(a, v, red);
+  double v[7];
+  block_grid_sum<7>(a, v, red);
   if (threadIdx.x == 0) {
-    q.p2[(size_t)b * 4 + 0] = v[0];
-    q.p2[(size_t)b * 4 + 1] = v[1];
+    double* out = q.p1 + (size_t)b * 8;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) out[k] = v[k];
   }
 }
 
-// Finish pass 2: the edot quadratic solve for the amplitude scale.
-__device__ __forceinline__ void fin2_body(const ForceParams& q, double* red) {
+// The totals (fixed order), the mass-weighted mean and the edot quadratic
+// solve for the amplitude scale: scal = (mean_x, mean_y, scale, m0, m1).
+__device__ __forceinline__ void fin_body(const ForceParams& q, double* red) {
   if (q.clock->done) return;
-  double v[2] = {0.0, 0.0};
+  double v[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < q.nblk; b += blockDim.x) {
-    v[0] += q.p2[b * 4 + 0];
-    v[1] += q.p2[b * 4 + 1];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) v[k] += q.p1[b * 8 + k];
   }
-  block_sum<2>(v, red);
+  block_sum<7>(v, red);
   if (threadIdx.x == 0) {
+    const double mean_x = v[1] / v[0], mean_y = v[2] / v[0];
     const double ncell = (double)q.ny * (double)q.nx;
-    const double m0 = v[0] / ncell, m1 = v[1] / ncell;
+    const double m0 = q.clock->dt * (v[3] - 0.5 * (mean_x * v[1] + mean_y * v[2])) / ncell;
+    const double m1 = (v[6] - (mean_x * v[4] + mean_y * v[5])) / ncell;
     const double dedt = q.clock->power;
     const double root = sqrt(m1 * m1 + 4.0 * m0 * dedt);
     double scale = m1 >= 0.0 ? 2.0 * dedt / (m1 + root) : (root - m1) / (2.0 * m0);
     if (!(m0 > 1e-30)) scale = NAN;
+    q.scal[0] = mean_x;
+    q.scal[1] = mean_y;
     q.scal[2] = scale;
     q.scal[3] = m0;
     q.scal[4] = m1;
@@ -465,7 +443,7 @@ __device__ __forceinline__ void kick_body(const ForceParams& q, int b, int nb, d
       for (int c = 3; c < q.nv; ++c) after[k * q.nv + c] = u[c];
     }
     const R rf = rho < dfloor ? dfloor : rho;
-    u[0] = rf;
+    if (rf != rho) u[0] = rf;  // the density is rewritten only where the floor applies
     u[1] = m1;
     u[2] = m2;
     if (q.want_cfl) {
@@ -493,25 +471,14 @@ __global__ void render_kernel(RenderParams q) {
 }
 
 template <typename R>
-__global__ void force_sum1_kernel(ForceParams q) {
-  __shared__ double red[32 * 3];
-  sum1_body<R>(q, blockIdx.x, red);
+__global__ void force_moments_kernel(ForceParams q) {
+  __shared__ double red[32 * 7];
+  moments_body<R>(q, blockIdx.x, red);
 }
 
-__global__ void force_fin1_kernel(ForceParams q) {
-  __shared__ double red[32 * 3];
-  fin1_body(q, red);
-}
-
-template <typename R>
-__global__ void force_sum2_kernel(ForceParams q) {
-  __shared__ double red[32 * 2];
-  sum2_body<R>(q, blockIdx.x, red);
-}
-
-__global__ void force_fin2_kernel(ForceParams q) {
-  __shared__ double red[32 * 2];
-  fin2_body(q, red);
+__global__ void force_fin_kernel(ForceParams q) {
+  __shared__ double red[32 * 7];
+  fin_body(q, red);
 }
 
 template <typename R>
@@ -563,27 +530,15 @@ __global__ void render_batch_kernel(const RenderParams* __restrict__ q, const in
 }
 
 template <typename R>
-__global__ void force_sum1_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
-  __shared__ double red[32 * 3];
+__global__ void force_moments_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
+  __shared__ double red[32 * 7];
   const int i = batch_solve_of(off, n, blockIdx.x);
-  sum1_body<R>(q[i], blockIdx.x - off[i], red);
+  moments_body<R>(q[i], blockIdx.x - off[i], red);
 }
 
-__global__ void force_fin1_batch_kernel(const ForceParams* __restrict__ q) {
-  __shared__ double red[32 * 3];
-  fin1_body(q[blockIdx.x], red);
-}
-
-template <typename R>
-__global__ void force_sum2_batch_kernel(const ForceParams* __restrict__ q, const int* __restrict__ off, int n) {
-  __shared__ double red[32 * 2];
-  const int i = batch_solve_of(off, n, blockIdx.x);
-  sum2_body<R>(q[i], blockIdx.x - off[i], red);
-}
-
-__global__ void force_fin2_batch_kernel(const ForceParams* __restrict__ q) {
-  __shared__ double red[32 * 2];
-  fin2_body(q[blockIdx.x], red);
+__global__ void force_fin_batch_kernel(const ForceParams* __restrict__ q) {
+  __shared__ double red[32 * 7];
+  fin_body(q[blockIdx.x], red);
 }
 
 template <typename R>
@@ -948,12 +903,9 @@ int kick_blocks(int64_t ncell) {
 
 cudaError_t launch_force_kick(int dtype, const ForceParams& q, cudaStream_t s) {
   const int g = kick_blocks((int64_t)q.ny * q.nx);
-  if (dtype == JX_F64) force_sum1_kernel<double><<<q.nblk, kReduceThreads, 0, s>>>(q);
-  else force_sum1_kernel<float><<<q.nblk, kReduceThreads, 0, s>>>(q);
-  force_fin1_kernel<<<1, kReduceThreads, 0, s>>>(q);
-  if (dtype == JX_F64) force_sum2_kernel<double><<<q.nblk, kReduceThreads, 0, s>>>(q);
-  else force_sum2_kernel<float><<<q.nblk, kReduceThreads, 0, s>>>(q);
-  force_fin2_kernel<<<1, kReduceThreads, 0, s>>>(q);
+  if (dtype == JX_F64) force_moments_kernel<double><<<q.nblk, kReduceThreads, 0, s>>>(q);
+  else force_moments_kernel<float><<<q.nblk, kReduceThreads, 0, s>>>(q);
+  force_fin_kernel<<<1, kReduceThreads, 0, s>>>(q);
   if (dtype == JX_F64) force_kick_kernel<double><<<g, kReduceThreads, 0, s>>>(q);
   else force_kick_kernel<float><<<g, kReduceThreads, 0, s>>>(q);
   return cudaGetLastError();
@@ -974,12 +926,9 @@ cudaError_t launch_render_batch(int dtype, const RenderParams* q, const int* off
 cudaError_t launch_force_kick_batch(int dtype, const ForceParams* q, int n, const int* off_sum, int sum_work,
                                     const int* off_kick, int kick_work, cudaStream_t s) {
   if (n < 1) return cudaSuccess;
-  if (dtype == JX_F64) force_sum1_batch_kernel<double><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
-  else force_sum1_batch_kernel<float><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
-  force_fin1_batch_kernel<<<n, kReduceThreads, 0, s>>>(q);
-  if (dtype == JX_F64) force_sum2_batch_kernel<double><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
-  else force_sum2_batch_kernel<float><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
-  force_fin2_batch_kernel<<<n, kReduceThreads, 0, s>>>(q);
+  if (dtype == JX_F64) force_moments_batch_kernel<double><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  else force_moments_batch_kernel<float><<<sum_work, kReduceThreads, 0, s>>>(q, off_sum, n);
+  force_fin_batch_kernel<<<n, kReduceThreads, 0, s>>>(q);
   if (dtype == JX_F64) force_kick_batch_kernel<double><<<kick_work, kReduceThreads, 0, s>>>(q, off_kick, n);
   else force_kick_batch_kernel<float><<<kick_work, kReduceThreads, 0, s>>>(q, off_kick, n);
   return cudaGetLastError();

@@ -39,8 +39,7 @@ struct ForceParams {
   const void* U;   // state read by the sums
   void* Uw;        // state written by the kick (same buffer)
   const void* raw;
-  double* p1;      // pass-1 partials (4 per block)
-  double* p2;      // pass-2 partials (4 per block)
+  double* p1;      // normalisation-moment partials (8 per block)
   double* scal;    // mean_x, mean_y, scale, m0, m1
   double* partials;  // CFL partials
   WsHeader* header;

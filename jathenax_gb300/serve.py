@@ -44,6 +44,7 @@ class Request:
     finished: float = None
     cycles: int = 0
     error: str = None
+    served_dtype: str = None  # the precision the server ran it in (see served_dtype)
     result: object = field(default=None, repr=False)
 
 
@@ -66,12 +67,51 @@ def make_stream(n, rate, seed=0, side_range=(64, 2048), tlim_range=(0.2, 3.0), f
     return out
 
 
-# Stage tiles of a served request: the 32 x 16 shared-memory tile in both
-# precisions. Served grids are small (64..2048) and a request's latency is
-# the length of its step chain, so the tile that 256 threads finish together
-# beats the register-marching tile, which one warp walks row by row (measured:
-# 2.5x lower p50 and 1.45x more solves/s under load).
+# Stage tile of a request built without a tile choice (build_solve's
+# default): the 32 x 16 shared-memory tile in both precisions.
 SERVING_TILES = {"float32": (32, 16), "float64": (32, 16)}
+
+# Size classes of served grids, for the tuned tiles: (largest side of the
+# class, side of its probe grids, probe solves). The bounds split the served
+# 64..2048 range into three geometric thirds.
+SIZE_CLASSES = ((203, 114, 8), (645, 362, 4), (1 << 30, 1149, 2))
+
+
+def size_class(side):
+    return next(i for i, (top, _, _) in enumerate(SIZE_CLASSES) if side <= top)
+
+
+# Float32 precision guard: a float32 request of a (problem, reconstruction)
+# pair listed here is served in float64 when its end time exceeds the listed
+# one (0: always). Beyond these end times the float32 result differs from the
+# float64 one by more than 1e-5 in L1 density somewhere in the measured set.
+# Two mechanisms, both properties of the flows and limiters rather than of
+# float32 arithmetic as such: the shear layers (and, later, the waves) are
+# chaotic, so any rounding difference grows - a float64 run perturbed in its
+# 15th digit drifts from the unperturbed one by the same factors; and PPMX's
+# smooth-extremum limiter takes discrete branches (curvature signs, the
+# 1e-12 relative threshold, the extremum test on exactly equal neighbours)
+# that these symmetric set-ups put on exact ties, which rounding moves.
+# Measured on GB300 with `bench.py --precision-sweep` (every problem x
+# reconstruction x Riemann solver, sides 64/85/128/256) at end times
+# 0.5 ... 3; a pair is kept in float32 up to the largest end time at which
+# every solver and side stayed below 2e-6 (five times under the bar).
+FP32_TLIM_MAX = {
+    ("kh", "plm"): 0.5, ("kh", "ppm4"): 0.5, ("kh", "wenoz"): 0.5, ("kh", "ppmx"): 0.0,
+    ("smooth", "ppmx"): 0.5, ("smooth", "wenoz"): 0.5,
+    ("turbulence", "plm"): 0.5, ("turbulence", "ppmx"): 0.0,
+}
+
+
+def served_dtype(req, dtype=None, guard=True):
+    """The precision a request is served in: `dtype` if given, else the
+    requested one, with float32 promoted to float64 where FP32_TLIM_MAX says."""
+    chosen = dtype or req.dtype
+    if guard and chosen == "float32":
+        limit = FP32_TLIM_MAX.get((req.problem, req.reconstruct))
+        if limit is not None and req.tlim > limit:
+            return "float64"
+    return chosen
 
 
 def _device_state(problem, n):
@@ -153,22 +193,58 @@ def footprint_bytes(req, dtype=None):
 
 
 class Server:
-    """Continuous-batching request loop with an HBM admission budget."""
+    """Continuous-batching request loop with an HBM admission budget.
 
-    def __init__(self, budget_bytes=150e9, tile=None, steps_per_tick=4, blocks_per_sm=0,
-                 max_live=1024, keep_results=False, dtype=None, builder=None):
+    ``tile``: a fixed stage tile for every request, None for SERVING_TILES,
+    or "auto" (default): the autotuner's choice per (precision, size class,
+    reconstruction), tuned on probe grids the first time such a request is
+    built (cached per GPU model; :meth:`warmup` tunes every class up front).
+    ``guard``: serve float32 requests in float64 where FP32_TLIM_MAX says.
+    """
+
+    def __init__(self, budget_bytes=150e9, tile="auto", steps_per_tick=4, blocks_per_sm=0,
+                 max_live=1024, keep_results=False, dtype=None, builder=None, guard=True):
         self.budget = float(budget_bytes)
-        self.tile = tile  # None: SERVING_TILES by precision
+        self.tile = tile
         self.steps_per_tick = steps_per_tick
         self.blocks_per_sm = blocks_per_sm
         self.max_live = max_live
         self.keep_results = keep_results
         self.dtype = dtype  # serve every request in this precision (None: as requested)
+        self.guard = guard
         self.builder = builder or build_solve  # (request, tile, clock, dtype) -> Solve
+        self.tuned = {}  # (precision, size class, reconstruction) -> autotune result
+
+    def dtype_for(self, req):
+        return served_dtype(req, self.dtype, self.guard)
+
+    def tile_for(self, req):
+        """The stage tile request `req` is served with."""
+        if self.tile != "auto":
+            return tuple(self.tile) if self.tile is not None else SERVING_TILES[self.dtype_for(req)]
+        dtype = self.dtype_for(req)
+        key = (dtype, size_class(req.side), req.reconstruct)
+        if key not in self.tuned:
+            from . import autotune
+            _, side, count = SIZE_CLASSES[key[1]]
+            self.tuned[key] = autotune.tune(dtype, req.reconstruct, "roe", 4, side, count=count)
+        return tuple(self.tuned[key]["tile"])
+
+    def tile_table(self):
+        """{"float32/class0/ppm4": {"tile": [...], "knobs": {...}}, ...} of the tiles tuned so far."""
+        return {f"{d}/class{c}/{r}": {"tile": v["tile"], "knobs": v["knobs"]}
+                for (d, c, r), v in sorted(self.tuned.items())}
 
     def warmup(self):
-        """Serve :func:`warmup_requests` once (untimed) to load every kernel."""
+        """Serve :func:`warmup_requests` once (untimed) to load every kernel
+        and, with automatic tiles, tune every size class and reconstruction."""
         dtypes = (self.dtype,) if self.dtype else ("float32", "float64")
+        if self.tile == "auto":
+            for dtype in dtypes:
+                for top, side, _ in SIZE_CLASSES:
+                    for recon in RECONS:
+                        self.tile_for(Request(rid=-1, arrival=0.0, problem="kh", side=min(top, side),
+                                              reconstruct=recon, rsolver="roe", tlim=0.0, dtype=dtype, seed=1))
         self.run(warmup_requests(dtypes))
 
     def run(self, requests):
@@ -223,13 +299,14 @@ class Server:
         while pending or live or retiring or previous:
             now = time.perf_counter() - t0
             while (pending and pending[0].arrival <= now and free_slots
-                   and in_use + footprint_bytes(pending[0], self.dtype) <= self.budget):
+                   and in_use + footprint_bytes(pending[0], self.dtype_for(pending[0])) <= self.budget):
                 req = pending.popleft()
                 slot = free_slots.pop()
-                solve = self.builder(req, self.tile, clock=bank.slot(slot), dtype=self.dtype)
+                req.served_dtype = self.dtype_for(req)
+                solve = self.builder(req, self.tile_for(req), clock=bank.slot(slot), dtype=req.served_dtype)
                 req.admitted = time.perf_counter() - t0
                 live.append((req, solve, slot))
-                in_use += footprint_bytes(req, self.dtype)
+                in_use += footprint_bytes(req, req.served_dtype)
                 peak_bytes = max(peak_bytes, in_use)
                 changed = True
             current = None
@@ -247,7 +324,7 @@ class Server:
             keep = []
             for entry in retiring:
                 if finish(entry, wait=not live and previous is None):
-                    in_use -= footprint_bytes(entry[0], self.dtype)
+                    in_use -= footprint_bytes(entry[0], entry[0].served_dtype)
                 else:
                     keep.append(entry)
             retiring = keep
@@ -284,7 +361,7 @@ class Server:
                 wait = pending[0].arrival - (time.perf_counter() - t0)
                 if wait > 0:
                     time.sleep(min(wait, 0.01))
-                elif in_use + footprint_bytes(pending[0], self.dtype) > self.budget:
+                elif in_use + footprint_bytes(pending[0], self.dtype_for(pending[0])) > self.budget:
                     raise RuntimeError(f"request {pending[0].rid} does not fit in the HBM budget")
         t.cuda.synchronize()
         elapsed = time.perf_counter() - t0
@@ -295,6 +372,7 @@ class Server:
             "elapsed_s": elapsed, "solves_per_s": len(ok) / elapsed,
             "tts_p50_s": float(np.percentile(tts, 50)), "tts_p99_s": float(np.percentile(tts, 99)),
             "ticks": ticks, "peak_live": peak_live, "peak_bytes": peak_bytes,
+        "promoted_to_float64": sum(1 for r in requests if r.served_dtype != (self.dtype or r.dtype)),
         }
 
 
@@ -306,6 +384,7 @@ def run_serial(requests, dtype="float64", keep_results=False):
     for req in requests:
         solve = build_solve(req, dtype=dtype)
         solve.run(steps_per_sync=32)
+        req.cycles = solve.state().cycle
         if keep_results:
             req.result = solve.S.cpu().numpy()
         del solve

@@ -64,6 +64,23 @@ class Solve:
         _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.ws),
                   self.nbytes, _lib.stream_handle())
 
+    def set_tile(self, tile):
+        """Switch the stage tile (see make_desc's ``tile``) of a live solve.
+
+        The workspace grows if the new tile needs more CFL partial slots, the
+        partials are recomputed from the current state and any captured graph
+        is dropped. Float32 results do not depend on the tile; float64 results
+        agree across tiles to rounding.
+        """
+        self.desc.tile_x, self.desc.tile_y = int(tile[0]), int(tile[1])
+        size = ctypes.c_size_t()
+        _lib.call("jx_workspace_bytes", ctypes.byref(self.desc), ctypes.byref(size))
+        if size.value > self.nbytes:
+            self.ws, self.nbytes = _lib.workspace(self.desc)
+        self.graph, self.graph_steps = None, 0
+        _lib.call("jx_cfl_partials", ctypes.byref(self.desc), _lib.ptr(self.S), _lib.ptr(self.ws),
+                  self.nbytes, _lib.stream_handle())
+
     # -- enqueueing -----------------------------------------------------------
     def enqueue_step(self, clock=None):
         """Enqueue one full cycle (no SGS hook) on the current stream."""
