@@ -93,13 +93,16 @@ def size_class(side):
 # 1e-12 relative threshold, the extremum test on exactly equal neighbours)
 # that these symmetric set-ups put on exact ties, which rounding moves.
 # Measured on GB300 with `bench.py --precision-sweep` (every problem x
-# reconstruction x Riemann solver, sides 64/85/128/256) at end times
-# 0.5 ... 3; a pair is kept in float32 up to the largest end time at which
-# every solver and side stayed below 2e-6 (five times under the bar).
+# reconstruction x Riemann solver, sides 64/85/128/256, end times 0.5, 1,
+# ..., 3); a pair is kept in float32 up to the largest end time at which
+# every solver and side stayed below 2e-6 (five times under the bar). Pairs
+# not listed stayed below it to t = 3. PPMX on the shear layer and in driven
+# turbulence exceeds the bar already at t = 0.5.
 FP32_TLIM_MAX = {
-    ("kh", "plm"): 0.5, ("kh", "ppm4"): 0.5, ("kh", "wenoz"): 0.5, ("kh", "ppmx"): 0.0,
-    ("smooth", "ppmx"): 0.5, ("smooth", "wenoz"): 0.5,
-    ("turbulence", "plm"): 0.5, ("turbulence", "ppmx"): 0.0,
+    ("kh", "dc"): 2.5, ("kh", "plm"): 1.0, ("kh", "ppm4"): 0.5, ("kh", "ppmx"): 0.0, ("kh", "wenoz"): 1.0,
+    ("smooth", "ppm4"): 2.5, ("smooth", "ppmx"): 1.0, ("smooth", "wenoz"): 0.5,
+    ("turbulence", "plm"): 2.0, ("turbulence", "ppm4"): 1.0, ("turbulence", "ppmx"): 0.0,
+    ("turbulence", "wenoz"): 2.5,
 }
 
 

@@ -105,7 +105,7 @@ def test_guarded_float32_results_stay_within_1e5_of_float64():
     float64, and the at-risk ones were promoted."""
     from jathenax_gb300.diagnostics import relative_l1
     from jathenax_gb300.serve import FP32_TLIM_MAX, Server, build_solve, make_stream
-    reqs = make_stream(30, 800.0, seed=33, side_range=(48, 160), tlim_range=(0.1, 1.2), fp32_fraction=1.0)
+    reqs = make_stream(30, 800.0, seed=33, side_range=(64, 160), tlim_range=(0.1, 1.2), fp32_fraction=1.0)
     stats = Server(budget_bytes=4e9, tile=(32, 16), steps_per_tick=8, keep_results=True).run(reqs)
     assert stats["completed"] == len(reqs)
     at_risk = [r for r in reqs if r.tlim > FP32_TLIM_MAX.get((r.problem, r.reconstruct), 1e30)]
