@@ -24,7 +24,6 @@
 #include "jx_device.cuh"
 #include "jx_internal.h"
 #include "jx_stage_fast.cuh"
-#include "jx_stage_march2.cuh"
 
 #include <utility>
 
@@ -487,10 +486,6 @@ template <typename R, int RECON, int RS, int NV, int NC>
 cudaError_t launch_march_nc(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (sizeof(R) == 4 && NC > 1) {
     const int form = march_form(p);
-    // Float32 PPM4 + Roe, two columns per lane, lean form: two tiles per
-    // warp as float32 pairs (jx_stage_march2.cuh), the same bits.
-    if constexpr (RECON == JX_PPM4 && RS == JX_ROE && NC == 2)
-      if (form != kMarchGeneric) return launch_march_pairs<NV>(p, ntiles, form == kMarchLeanBlend, s);
     if (form == kMarchLeanBlend) {
       stage_kernel_march<R, RECON, RS, NV, NC, kMarchLeanBlend><<<blocks, threads, 0, s>>>(p, ntiles);
       return cudaGetLastError();
