@@ -21,9 +21,11 @@ float64 results agree across knobs to rounding (marching and shared-memory
 kernels contract different products). Float64 marches with two columns per
 lane only.
 
-Each candidate runs ``warmup`` untimed and ``repeats`` x ``steps`` timed
-batched cycles (CUDA events); its time is the median repeat, and the SM
-clock (``nvidia-smi``) is read before and after the search. Probe-grid
+Each candidate starts from the same states and clocks (restored before it
+runs, so a solve that reaches its end time during the search does so in
+every candidate alike), runs ``warmup`` untimed and ``repeats`` x ``steps``
+timed batched cycles (CUDA events); its time is the median repeat, and the
+SM clock (``nvidia-smi``) is read before and after the search. Probe-grid
 results (:func:`tune`) are cached per GPU model in memory and in
 ``$JATHENAX_GB300_CACHE`` (default ``~/.cache/jathenax_gb300/autotune.json``).
 """
@@ -89,8 +91,10 @@ def time_batch(batch, steps, repeats, warmup):
 
 def tune_batch(solves, tiles=None, blocks_per_sm=BLOCKS_PER_SM, steps=10, repeats=2, warmup=2):
     """Pick the knobs for one particular set of solves by timing the batched
-    cycle itself. The solves are retiled in place (Solve.set_tile) and advanced
-    by the timed cycles; build fresh ones for the real run.
+    cycle itself. The solves are retiled in place (Solve.set_tile); their
+    states and clocks are put back before every candidate and at the end, but
+    forcing caches and CFL partials are not, so build fresh ones for the real
+    run.
 
     Returns {"knobs", "tile", "blocks_per_sm", "ms_per_step", "trials",
     "clock_mhz", "timing"} (not cached: the answer belongs to the solve set).
@@ -100,17 +104,27 @@ def tune_batch(solves, tiles=None, blocks_per_sm=BLOCKS_PER_SM, steps=10, repeat
     if tiles is None:
         tiles = tiles_for("float32" if dtypes == {"float32"} else "float64")
     clock_before = sm_clock_mhz()
+    saved = [(s.S.clone(), s.clock.clone()) for s in solves]
+
+    def restore():
+        for s, (state, clock) in zip(solves, saved):
+            s.S.copy_(state)
+            s.clock.copy_(clock)
+
     trials = []
     for tile in tiles:
+        restore()
         try:
             for s in solves:
                 s.set_tile(tile)
         except (ValueError, RuntimeError):  # e.g. the tile does not fit in shared memory
             continue
         for bps in blocks_per_sm:
+            restore()
             runs = time_batch(Batch(solves, blocks_per_sm=bps), steps, repeats, warmup)
             trials.append(dict(knobs(tile, bps), ms_per_step=statistics.median(runs),
                                repeats_ms=[round(r, 4) for r in runs]))
+    restore()
     if not trials:
         raise RuntimeError("no autotuning candidate could run")
     best = min(trials, key=lambda r: r["ms_per_step"])

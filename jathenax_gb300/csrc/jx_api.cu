@@ -123,14 +123,26 @@ int march_occupancy(const jx_desc* d, int nc) {
 // Rows of an automatic marching tile: the height whose tiles, spread over
 // the resident warp slots of the device, finish soonest. A tile of h rows
 // costs about h + 2.5 row-updates (the 6 leading rows of the walk do the y
-// work only); the grid runs in ceil(tiles / slots) rounds.
+// work only); the grid runs in ceil(tiles / slots) rounds. Besides a fixed
+// list the candidates include the shortest height whose tiles all fit in one
+// round (every warp walks one tall tile; e.g. 121 rows at 4096^2 with 16
+// resident warps per SM: 2414 tiles on 2432 slots).
 int march_rows(const jx_desc* d, int nc) {
   static const int kRows[] = {8, 12, 16, 24, 32, 48, 64};
   const int64_t slots = (int64_t)sm_count() * march_occupancy(d, nc) * kMarchWarps;
   const int64_t cols = (d->nx + march_tile_x(nc) - 1) / march_tile_x(nc);
+  int cand[8];
+  int ncand = 0;
+  for (int h : kRows) cand[ncand++] = h;
+  const int64_t rows_per_round = slots / cols;  // tile rows that fit in one round
+  if (rows_per_round >= 1) {
+    const int64_t h1 = (d->ny + rows_per_round - 1) / rows_per_round;
+    if (h1 > kRows[6] && h1 <= d->ny) cand[ncand++] = (int)h1;
+  }
   int best = kRows[0];
   double best_cost = 1e300;
-  for (int h : kRows) {
+  for (int i = 0; i < ncand; ++i) {
+    const int h = cand[i];
     const int64_t tiles = cols * ((d->ny + h - 1) / h);
     const int64_t rounds = (tiles + slots - 1) / slots;
     const double cost = (double)rounds * (h + 2.5);

@@ -240,15 +240,23 @@ class Server:
 
     def warmup(self):
         """Serve :func:`warmup_requests` once (untimed) to load every kernel
-        and, with automatic tiles, tune every size class and reconstruction."""
+        and, with automatic tiles, tune every size class and reconstruction,
+        in every precision a request can be served in (float64 too where the
+        guard may promote float32 requests)."""
         dtypes = (self.dtype,) if self.dtype else ("float32", "float64")
+        if self.guard and "float32" in dtypes and "float64" not in dtypes:
+            dtypes += ("float64",)
         if self.tile == "auto":
             for dtype in dtypes:
                 for top, side, _ in SIZE_CLASSES:
                     for recon in RECONS:
                         self.tile_for(Request(rid=-1, arrival=0.0, problem="kh", side=min(top, side),
                                               reconstruct=recon, rsolver="roe", tlim=0.0, dtype=dtype, seed=1))
-        self.run(warmup_requests(dtypes))
+        forced, self.dtype = self.dtype, None  # each warm-up request in its own precision
+        try:
+            self.run(warmup_requests(dtypes))
+        finally:
+            self.dtype = forced
 
     def run(self, requests):
         """Serve `requests` (arrival-ordered or not); returns a stats dict.
