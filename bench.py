@@ -781,7 +781,7 @@ def bench_reference(args, world, rank):
 def bench_precision_sweep(args):
     """Float32 vs float64 L1 density error per (problem, method, side, end time) as served
     (the serving set-ups, build_solve), one JSON line each: the evidence behind serve.py's
-    float32 precision guard (FP32_TLIM_MAX)."""
+    float32 precision guard (serve.FP32_ERR)."""
     import torch
     from jathenax_gb300.diagnostics import relative_l1
     from jathenax_gb300.serve import PROBLEMS, RECONS, SOLVERS, Request, build_solve

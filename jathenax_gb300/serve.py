@@ -81,38 +81,80 @@ def size_class(side):
     return next(i for i, (top, _, _) in enumerate(SIZE_CLASSES) if side <= top)
 
 
-# Float32 precision guard: a float32 request of a (problem, reconstruction)
-# pair listed here is served in float64 when its end time exceeds the listed
-# one (0: always). Beyond these end times the float32 result differs from the
-# float64 one by more than 1e-5 in L1 density somewhere in the measured set.
-# Two mechanisms, both properties of the flows and limiters rather than of
-# float32 arithmetic as such: the shear layers (and, later, the waves) are
-# chaotic, so any rounding difference grows - a float64 run perturbed in its
-# 15th digit drifts from the unperturbed one by the same factors; and PPMX's
-# smooth-extremum limiter takes discrete branches (curvature signs, the
-# 1e-12 relative threshold, the extremum test on exactly equal neighbours)
-# that these symmetric set-ups put on exact ties, which rounding moves.
-# Measured on GB300 with `bench.py --precision-sweep` (every problem x
-# reconstruction x Riemann solver, sides 64/85/128/256, end times 0.5, 1,
-# ..., 3); a pair is kept in float32 up to the largest end time at which
-# every solver and side stayed below 2e-6 (five times under the bar). Pairs
-# not listed stayed below it to t = 3. PPMX on the shear layer and in driven
-# turbulence exceeds the bar already at t = 0.5.
-FP32_TLIM_MAX = {
-    ("kh", "dc"): 2.5, ("kh", "plm"): 1.0, ("kh", "ppm4"): 0.5, ("kh", "ppmx"): 0.0, ("kh", "wenoz"): 1.0,
-    ("smooth", "ppm4"): 2.5, ("smooth", "ppmx"): 1.0, ("smooth", "wenoz"): 0.5,
-    ("turbulence", "plm"): 2.0, ("turbulence", "ppm4"): 1.0, ("turbulence", "ppmx"): 0.0,
-    ("turbulence", "wenoz"): 2.5,
+# Float32 precision guard. FP32_ERR holds, per (problem, reconstruction),
+# the worst float32-vs-float64 L1 density error measured over the three
+# Riemann solvers at end times FP32_ERR_TLIMS: row 0 the worst over sides 64,
+# 85, 128 and 256, row 1 at side 512 (GB300, `bench.py --precision-sweep`
+# and `--precision-sweep --n 512`). Two mechanisms make it grow, both
+# properties of the flows and limiters rather than of float32 arithmetic as
+# such: the shear layers (and, later, the waves) are chaotic, so any rounding
+# difference grows - a float64 run perturbed in its 15th digit drifts from
+# the unperturbed one by the same factors; and PPMX's smooth-extremum
+# limiter takes discrete branches (curvature signs, the 1e-12 relative
+# threshold, the extremum test on exactly equal neighbours) that these
+# symmetric set-ups put on exact ties, which rounding moves.
+FP32_ERR_TLIMS = (0.5, 1.0, 1.5, 2.0, 2.5, 3.0)
+FP32_ERR = {
+    ("kh", "dc"): ((1.3e-07, 1.8e-07, 3.8e-07, 8.7e-07, 1.6e-06, 2.5e-06),
+                   (3.8e-07, 6.1e-07, 1.4e-06, 1.9e-06, 3.3e-06, 8.7e-06)),
+    ("kh", "plm"): ((2.9e-07, 1.7e-06, 7.5e-06, 2.1e-05, 8.8e-05, 3.2e-04),
+                    (7.4e-07, 1.3e-06, 4.8e-06, 1.4e-05, 8.0e-05, 2.8e-04)),
+    ("kh", "ppm4"): ((5.4e-07, 2.3e-06, 2.1e-05, 3.8e-05, 7.7e-05, 2.5e-04),
+                     (8.5e-07, 2.2e-06, 1.4e-05, 4.7e-05, 1.7e-04, 7.0e-04)),
+    ("kh", "ppmx"): ((2.2e-04, 1.3e-03, 5.9e-03, 9.0e-03, 1.2e-02, 2.0e-02),
+                     (1.0e-06, 4.1e-06, 6.9e-05, 3.4e-04, 7.5e-04, 1.4e-03)),
+    ("kh", "wenoz"): ((3.7e-07, 1.4e-06, 1.1e-05, 2.8e-05, 1.3e-04, 5.1e-04),
+                      (7.0e-07, 1.4e-06, 6.5e-06, 1.6e-05, 4.0e-05, 2.2e-04)),
+    ("smooth", "dc"): ((6.9e-08, 6.9e-08, 8.1e-08, 7.6e-08, 7.5e-08, 7.3e-08),
+                       (7.5e-08, 7.3e-08, 7.8e-08, 7.7e-08, 8.0e-08, 8.5e-08)),
+    ("smooth", "plm"): ((1.2e-07, 1.5e-07, 1.7e-07, 1.7e-07, 1.8e-07, 2.1e-07),
+                        (1.6e-07, 1.9e-07, 2.1e-07, 2.3e-07, 2.4e-07, 2.4e-07)),
+    ("smooth", "ppm4"): ((5.0e-07, 5.3e-07, 5.1e-07, 8.8e-07, 1.1e-06, 7.3e-05),
+                         (6.4e-07, 6.8e-07, 8.5e-07, 7.6e-06, 2.2e-05, 3.5e-05)),
+    ("smooth", "ppmx"): ((5.5e-07, 1.2e-06, 1.1e-05, 2.0e-04, 3.0e-04, 3.6e-04),
+                         (6.4e-07, 7.0e-07, 9.3e-06, 1.4e-04, 1.8e-04, 2.3e-04)),
+    ("smooth", "wenoz"): ((2.2e-07, 3.8e-06, 7.5e-05, 5.2e-04, 5.4e-04, 7.5e-04),
+                          (2.7e-07, 3.2e-07, 3.6e-05, 2.8e-04, 4.3e-04, 5.1e-04)),
+    ("turbulence", "dc"): ((7.5e-08, 7.5e-08, 8.6e-08, 3.9e-07, 2.0e-07, 1.5e-07),
+                           (9.4e-08, 9.8e-08, 1.0e-07, 1.0e-07, 1.1e-07, 1.1e-07)),
+    ("turbulence", "plm"): ((1.3e-07, 1.5e-07, 1.7e-07, 1.6e-06, 8.9e-05, 1.3e-04),
+                            (1.8e-07, 2.0e-07, 2.2e-07, 2.3e-07, 2.4e-07, 2.8e-07)),
+    ("turbulence", "ppm4"): ((4.4e-07, 5.3e-07, 3.5e-06, 7.0e-05, 8.2e-05, 1.1e-04),
+                             (7.5e-07, 1.2e-06, 1.4e-06, 1.5e-06, 1.2e-06, 1.1e-06)),
+    ("turbulence", "ppmx"): ((5.4e-06, 3.7e-05, 1.1e-04, 1.7e-04, 2.3e-04, 3.0e-04),
+                             (6.4e-07, 7.6e-07, 1.2e-06, 3.5e-06, 6.6e-06, 1.1e-05)),
+    ("turbulence", "wenoz"): ((2.3e-07, 2.6e-07, 3.0e-07, 3.3e-07, 5.3e-07, 2.7e-06),
+                              (2.8e-07, 3.3e-07, 3.7e-07, 4.0e-07, 4.3e-07, 5.8e-06)),
 }
+# Float32 is kept where the estimate stays at or under FP32_ERR_BAR, five
+# times below the 1e-5 L1 bar.
+FP32_ERR_BAR = 2e-6
+
+
+def fp32_error_estimate(problem, reconstruct, side, tlim):
+    """Estimated float32-vs-float64 L1 density error of a request: the worst
+    measured error (FP32_ERR) at any end time up to the first measured one
+    at or past `tlim`, over the measured sides up to the request's (row 0
+    only for sides up to 256), times (side / 512)^2 above 512 (the measured
+    growth on the shear layer is about 2-3x per doubling of the side at a
+    fixed end time; 4x is the margin for unmeasured sides). None where
+    nothing was measured (end times past 3, unknown problems)."""
+    rows = FP32_ERR.get((problem, reconstruct))
+    i = next((k for k, t in enumerate(FP32_ERR_TLIMS) if t >= tlim), None)
+    if rows is None or i is None:
+        return None
+    worst = max(rows[0][:i + 1]) if side <= 256 else max(max(rows[0][:i + 1]), max(rows[1][:i + 1]))
+    return worst * max(1.0, side / 512.0) ** 2
 
 
 def served_dtype(req, dtype=None, guard=True):
     """The precision a request is served in: `dtype` if given, else the
-    requested one, with float32 promoted to float64 where FP32_TLIM_MAX says."""
+    requested one, with float32 promoted to float64 where the guard's error
+    estimate (fp32_error_estimate) is unknown or above FP32_ERR_BAR."""
     chosen = dtype or req.dtype
     if guard and chosen == "float32":
-        limit = FP32_TLIM_MAX.get((req.problem, req.reconstruct))
-        if limit is not None and req.tlim > limit:
+        est = fp32_error_estimate(req.problem, req.reconstruct, req.side, req.tlim)
+        if est is None or est > FP32_ERR_BAR:
             return "float64"
     return chosen
 
@@ -202,7 +244,7 @@ class Server:
     or "auto" (default): the autotuner's choice per (precision, size class,
     reconstruction), tuned on probe grids the first time such a request is
     built (cached per GPU model; :meth:`warmup` tunes every class up front).
-    ``guard``: serve float32 requests in float64 where FP32_TLIM_MAX says.
+    ``guard``: serve float32 requests in float64 where served_dtype's error estimate says.
     """
 
     def __init__(self, budget_bytes=150e9, tile="auto", steps_per_tick=4, blocks_per_sm=0,

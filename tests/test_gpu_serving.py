@@ -104,11 +104,12 @@ def test_guarded_float32_results_stay_within_1e5_of_float64():
     float32 is within 1e-5 (L1 density, relative) of the same request run in
     float64, and the at-risk ones were promoted."""
     from jathenax_gb300.diagnostics import relative_l1
-    from jathenax_gb300.serve import FP32_TLIM_MAX, Server, build_solve, make_stream
+    from jathenax_gb300.serve import FP32_ERR_BAR, Server, build_solve, fp32_error_estimate, make_stream
     reqs = make_stream(30, 800.0, seed=33, side_range=(64, 160), tlim_range=(0.1, 1.2), fp32_fraction=1.0)
     stats = Server(budget_bytes=4e9, tile=(32, 16), steps_per_tick=8, keep_results=True).run(reqs)
     assert stats["completed"] == len(reqs)
-    at_risk = [r for r in reqs if r.tlim > FP32_TLIM_MAX.get((r.problem, r.reconstruct), 1e30)]
+    estimates = [fp32_error_estimate(r.problem, r.reconstruct, r.side, r.tlim) for r in reqs]
+    at_risk = [r for r, e in zip(reqs, estimates) if e is None or e > FP32_ERR_BAR]
     assert at_risk and all(r.served_dtype == "float64" for r in at_risk)
     assert stats["promoted_to_float64"] == len(at_risk)
     served32 = [r for r in reqs if r.served_dtype == "float32"]

@@ -157,3 +157,33 @@ def test_native_ou_table_is_bitwise_the_oracle(args):
     native = G.modal_coefficients(modes, *args)
     oracle = F.ou_table(modes, *args)
     np.testing.assert_array_equal(native.view(np.uint64), oracle.view(np.uint64))
+
+
+def test_precision_guard_estimate():
+    """The serving guard's float32 error estimate: measured values for the
+    measured sides, side growth above 512, unknown past the measured end
+    times, and the promotions it implies."""
+    from jathenax_gb300.serve import FP32_ERR, FP32_ERR_BAR, Request, fp32_error_estimate, served_dtype
+    assert fp32_error_estimate("kh", "dc", 128, 0.3) == FP32_ERR[("kh", "dc")][0][0]
+    # End times between measured ones take the worst up to the next one.
+    assert fp32_error_estimate("kh", "ppm4", 200, 1.2) == max(FP32_ERR[("kh", "ppm4")][0][:3])
+    # Sides above 256 include the 512 row; above 512 the estimate grows as side^2.
+    e512 = fp32_error_estimate("kh", "dc", 512, 2.0)
+    assert e512 == max(max(FP32_ERR[("kh", "dc")][0][:4]), max(FP32_ERR[("kh", "dc")][1][:4]))
+    assert fp32_error_estimate("kh", "dc", 1024, 2.0) == pytest.approx(4 * e512)
+    assert fp32_error_estimate("kh", "dc", 100, 3.5) is None
+    assert fp32_error_estimate("kh", "unknown", 100, 1.0) is None
+
+    def req(problem, recon, side, tlim, dtype="float32"):
+        return Request(rid=0, arrival=0.0, problem=problem, side=side, reconstruct=recon, rsolver="hlle",
+                       tlim=tlim, dtype=dtype, seed=1)
+
+    assert served_dtype(req("kh", "ppmx", 64, 0.1)) == "float64"  # PPMX on the shear layer: always
+    assert served_dtype(req("smooth", "dc", 2048, 3.0)) == "float32"
+    assert served_dtype(req("kh", "dc", 1976, 2.24)) == "float64"
+    assert served_dtype(req("kh", "dc", 1976, 2.24), guard=False) == "float32"
+    assert served_dtype(req("kh", "ppmx", 64, 0.1, "float64")) == "float64"
+    assert served_dtype(req("smooth", "dc", 64, 0.1), dtype="float64") == "float64"
+    assert all(fp32_error_estimate(p, r, s, t) is None or
+               (fp32_error_estimate(p, r, s, t) <= FP32_ERR_BAR) == (served_dtype(req(p, r, s, t)) == "float32")
+               for (p, r) in FP32_ERR for s in (64, 300, 900) for t in (0.2, 1.1, 2.9))
