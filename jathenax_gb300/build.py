@@ -51,7 +51,9 @@ def build(verbose=False, ptxas_info=False, jobs=None):
     """Compile every kernel for sm_103a and link libjx.so; returns its path."""
     nvcc = nvcc_path()
     OBJDIR.mkdir(exist_ok=True)
-    sources = sorted(CSRC.glob("*.cu"))
+    # The longest translation units (the WENO-Z and PPMX kernels) go first,
+    # so that the pool does not end on one of them.
+    sources = sorted(CSRC.glob("*.cu"), key=lambda f: (0 if "wenoz" in f.stem else 1 if "ppmx" in f.stem else 2, f.name))
     host_sources = sorted(CSRC.glob("*.cpp"))
     flags = ["-Xptxas", "-v"] if ptxas_info else []
     jobs = jobs or min(len(sources) + len(host_sources), os.cpu_count() or 4)

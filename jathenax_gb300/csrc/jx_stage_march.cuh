@@ -16,8 +16,10 @@
 //     edge and one flux per row);
 //   * row j-3 is then updated (divergence, RK combine, drag, floor) and
 //     written for the tile's 58 columns.
-// There is no shared memory and no barrier; a warp's CFL partial (the exact
-// maximum over its tile) goes to the workspace slot of its tile. Arithmetic
+// There is no barrier and no data shared between lanes through memory (on
+// float32 tiles of 24 rows or more each lane stages its own rows in a
+// shared-memory ring, see kRingU); a warp's CFL partial (the exact maximum
+// over its tile) goes to the workspace slot of its tile. Arithmetic
 // per cell is the same as in jx_stage_fast.cuh (same device functions in the
 // same order), so results agree with it to rounding.
 #pragma once
@@ -149,6 +151,56 @@ __device__ __forceinline__ void lane_cells(const Cell4<R> (&own)[NC], Cell4<R> (
   lane_cells_impl<NC, R, NV>(own, E, std::make_integer_sequence<int, NC + 4>{});
 }
 
+// Row ring of the float32 single-solve walk on tall tiles: rows of U arrive
+// by cp.async three rows ahead of their use and rows of V three rows ahead
+// of the RK combine, into shared memory that only the copying lane reads
+// (slot [row][column h][lane], 16 bytes a cell, so a warp's accesses are
+// conflict-free). kRingU rows of U stay until the combine of the row has
+// read them too (its U then comes from the ring, not from L1/L2); kRingV
+// rows of V. No register holds a row in flight. Measured on GB300 at 4096²
+// (ppm4+roe, float32, RK3 stage 2): 0.2957 -> 0.2814 ms on 58 x 121 tiles,
+// 0.3144 -> 0.2792 ms on 90 x 106; on the 8-row tiles of a 1024² grid it
+// was 7 % slower (0.027 -> 0.029 ms), so tiles shorter than kRingMinRows
+// keep the register path. The bits are the same either way.
+constexpr int kRingU = 8, kRingV = 4, kRingAhead = 3, kRingMinRows = 24;
+template <int NC> __host__ __device__ constexpr int march_ring_bytes() { return (kRingU + kRingV) * NC * 32 * 16; }
+
+__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One cell (NV floats) from global to its ring slot.
+template <int NV>
+__device__ __forceinline__ void ring_copy(float4* slot, const float* g) {
+  if constexpr (NV == 4) {
+    cp_async_16(slot, g);
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async_4(reinterpret_cast<float*>(slot) + v, g + v);
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ Cell4<float> ring_read(const float4* slot) {
+  const float4 t = *slot;
+  Cell4<float> c;
+  c.v[0] = t.x;
+  c.v[1] = t.y;
+  c.v[2] = t.z;
+  c.v[3] = NV == 4 ? t.w : 0.0f;
+  return c;
+}
+
 // PREFETCH_V: issue L2 prefetches of the saved register two rows ahead of
 // the RK combine. Measured on GB300: it helps the batch kernel (12 resident
 // warps per SM, ensemble cycle -2.2 %) and costs the single-solve kernel
@@ -168,8 +220,8 @@ __device__ __forceinline__ void lane_cells(const Cell4<R> (&own)[NC], Cell4<R> (
 // instruction cache. Lanes whose columns are ghosts (or beyond a ragged right
 // edge) run the RK combine on a cell of their own tile and skip only the
 // store, so the combine has no divergent branch.
-template <typename R, int RECON, int RS, int NV, int NC, int FORM, bool PREFETCH_V>
-__device__ __forceinline__ void march_tile(const StageParams& p, int tile, int ntiles) {
+template <typename R, int RECON, int RS, int NV, int NC, int FORM, bool PREFETCH_V, bool RING = false>
+__device__ __forceinline__ void march_tile(const StageParams& p, int tile, int ntiles, float4* ring = nullptr) {
   using N = Num<R>;
   constexpr bool kLean = FORM != kMarchGeneric;
   constexpr int TX = march_tile_x(NC);
@@ -220,7 +272,17 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   R vmax0 = R(0), vmax1 = R(0);
   const int iters = TY + 6;
   Cell4<R> next[NC];
-  {
+  // Ring slots of this lane: U row t (t = it) at ringU(t, h), V at ringV(t, h).
+  auto ringU = [&](int t, int h) { return ring + ((t & (kRingU - 1)) * NC + h) * 32 + lane; };
+  auto ringV = [&](int t, int h) { return ring + (kRingU * NC + (t & (kRingV - 1)) * NC + h) * 32 + lane; };
+  if constexpr (RING) {
+    for (int t = 0; t < kRingAhead; ++t) {
+      const size_t row = (size_t)wrap_fast(y0 - 3 + t, p.ny) * p.nx;
+#pragma unroll
+      for (int h = 0; h < NC; ++h) ring_copy<NV>(ringU(t, h), U + (row + gx[h]) * NV);
+      cp_async_commit();
+    }
+  } else {
     const size_t row = (size_t)wrap_fast(y0 - 3, p.ny) * p.nx;
 #pragma unroll
     for (int h = 0; h < NC; ++h) next[h] = load_cell<R, NV>(U + (row + gx[h]) * NV);
@@ -231,6 +293,15 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
     const int j = y0 - 3 + it;
     // ---- y sweep of every column -------------------------------------------
     Cell4<R> Ay1[NC], lo[NC], hi[NC], Fy2[NC];
+    if constexpr (RING) {
+      // kRingAhead + it groups are committed: the prologue's kRingAhead
+      // (U rows 0 .. kRingAhead - 1) and one per earlier row. This row's U
+      // and the V the combine reads below (row it - 3) came in group it,
+      // so all but the kRingAhead - 1 newest groups must have landed.
+      cp_async_wait<kRingAhead - 1>();
+#pragma unroll
+      for (int h = 0; h < NC; ++h) next[h] = ring_read<NV>(ringU(it, h));
+    }
 #pragma unroll
     for (int h = 0; h < NC; ++h) {
       MarchColumn<R>& c = col[h];
@@ -240,7 +311,21 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
       c.W1 = c.W0;
       c.W0 = recover_cell<R, NV>(next[h], k.dfloor);
     }
-    {
+    if constexpr (RING) {
+      // U row it + 3 (only rows the walk reaches) and V of row it (a tile
+      // row the combine will update, three iterations from now).
+      if (it + kRingAhead < iters) {
+        const size_t row = (size_t)wrap_fast(j + kRingAhead, p.ny) * p.nx;
+#pragma unroll
+        for (int h = 0; h < NC; ++h) ring_copy<NV>(ringU(it + kRingAhead, h), U + (row + gx[h]) * NV);
+      }
+      if (it >= 3 && j < p.ny && it < TY + 3) {
+        const size_t row = (size_t)j * p.nx;
+#pragma unroll
+        for (int h = 0; h < NC; ++h) ring_copy<NV>(ringV(it, h), V + (row + (size_t)cx[h]) * NV);
+      }
+      cp_async_commit();
+    } else {
       // The row after this one (past the tile's last row: a wrapped row
       // that is never used, cheaper than a test).
       const size_t row = (size_t)wrap_fast(j + 1, p.ny) * p.nx;
@@ -366,9 +451,18 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
           const Cell4<R>& fl = F[h];
           const Cell4<R>& fr = F[h + 1];
           const Cell4<R>& w = col[h].W3;
-          Cell4<R> u = load_cell<R, NV>(U + cell * NV);
+          Cell4<R> u, vs;
+          if constexpr (RING) {
+            // Row r is walk row it - 3: its U is still in the ring (for a
+            // ghost lane that is the lane's own column, not cx: the result
+            // is not stored), its V landed with this row's group.
+            u = ring_read<NV>(ringU(it - 3, h));
+            vs = ring_read<NV>(ringV(it - 3, h));
+          } else {
+            u = load_cell<R, NV>(U + cell * NV);
+            vs = load_cell<R, NV>(V + cell * NV);
+          }
           u.v[0] = w.v[0];  // the floored density
-          Cell4<R> vs = load_cell<R, NV>(V + cell * NV);
           if (p.floor_v) vs.v[0] = N::lt(vs.v[0], k.dfloor) ? k.dfloor : vs.v[0];
           Cell4<R> un;
 #pragma unroll
@@ -411,6 +505,7 @@ __device__ __forceinline__ void march_tile(const StageParams& p, int tile, int n
   for (int it = 0; it < 6; ++it) walk_row(it, Flag<false>{});
 #pragma unroll 1
   for (int it = 6; it < iters; ++it) walk_row(it, Flag<true>{});
+  if constexpr (RING) cp_async_wait_all();
   if (p.want_cfl) {
     const double m0 = warp_nan_max(static_cast<double>(vmax0));
     const double m1 = warp_nan_max(static_cast<double>(vmax1));
@@ -447,13 +542,34 @@ template <typename R, int RECON, int NC> constexpr int march_batch_min_blocks() 
 }
 
 // One warp per tile; the block's warps take consecutive tiles.
-template <typename R, int RECON, int RS, int NV, int NC, int FORM>
+// RING (float32 only): the row ring above, march_smem bytes of dynamic
+// shared memory per block.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM, bool RING = false>
 __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, NC>()))
     stage_kernel_march(const StageParams p, int ntiles) {
   if (p.clock->done) return;
   const int tile = blockIdx.x * kMarchWarps + (threadIdx.x >> 5);
   if (tile >= ntiles) return;
-  march_tile<R, RECON, RS, NV, NC, FORM, false>(p, tile, ntiles);
+  if constexpr (RING && sizeof(R) == 4) {
+    extern __shared__ float4 march_ring[];
+    march_tile<R, RECON, RS, NV, NC, FORM, false, true>(p, tile, ntiles,
+                                                       march_ring + (threadIdx.x >> 5) * (march_ring_bytes<NC>() / 16));
+  } else {
+    march_tile<R, RECON, RS, NV, NC, FORM, false>(p, tile, ntiles);
+  }
+}
+
+template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
+
+// Let a ring kernel have the largest shared-memory carve-out (once per kernel).
+template <auto Kernel>
+void march_prefer_shared() {
+  static const bool done = [] {
+    cudaFuncSetAttribute(Kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaGetLastError();
+    return true;
+  }();
+  (void)done;
 }
 
 // Persistent batch kernel over marching tiles (see stage_kernel_batch): each
@@ -482,21 +598,27 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // only on request: its default is the shared-memory tile) always runs the
 // generic form with two columns per lane. One column per lane (a latency
 // choice for small grids) runs the generic form.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM>
+cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4) {
+    if (p.ty >= kRingMinRows) {
+      march_prefer_shared<stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>>();
+      stage_kernel_march<R, RECON, RS, NV, NC, FORM, true><<<blocks, threads, march_smem<NC>(), s>>>(p, ntiles);
+      return cudaGetLastError();
+    }
+  }
+  stage_kernel_march<R, RECON, RS, NV, NC, FORM><<<blocks, threads, 0, s>>>(p, ntiles);
+  return cudaGetLastError();
+}
+
 template <typename R, int RECON, int RS, int NV, int NC>
 cudaError_t launch_march_nc(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (sizeof(R) == 4 && NC > 1) {
     const int form = march_form(p);
-    if (form == kMarchLeanBlend) {
-      stage_kernel_march<R, RECON, RS, NV, NC, kMarchLeanBlend><<<blocks, threads, 0, s>>>(p, ntiles);
-      return cudaGetLastError();
-    }
-    if (form == kMarchLeanPlain) {
-      stage_kernel_march<R, RECON, RS, NV, NC, kMarchLeanPlain><<<blocks, threads, 0, s>>>(p, ntiles);
-      return cudaGetLastError();
-    }
+    if (form == kMarchLeanBlend) return launch_march_form<R, RECON, RS, NV, NC, kMarchLeanBlend>(p, blocks, threads, ntiles, s);
+    if (form == kMarchLeanPlain) return launch_march_form<R, RECON, RS, NV, NC, kMarchLeanPlain>(p, blocks, threads, ntiles, s);
   }
-  stage_kernel_march<R, RECON, RS, NV, NC, kMarchGeneric><<<blocks, threads, 0, s>>>(p, ntiles);
-  return cudaGetLastError();
+  return launch_march_form<R, RECON, RS, NV, NC, kMarchGeneric>(p, blocks, threads, ntiles, s);
 }
 
 // grid.x = number of tiles (one warp each); p.nc selects the columns per lane.
@@ -512,70 +634,54 @@ cudaError_t launch_march_one(const StageParams& p, dim3 grid, cudaStream_t s) {
   return launch_march_nc<R, RECON, RS, NV, 2>(p, blocks, threads, ntiles, s);
 }
 
-template <typename R, int RECON>
-cudaError_t launch_march_typed(int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
-  const bool three = p.nv == 3;
-  switch (rsolver) {
-    case JX_LLF: return three ? launch_march_one<R, RECON, JX_LLF, 3>(p, grid, s) : launch_march_one<R, RECON, JX_LLF, 4>(p, grid, s);
-    case JX_HLLE: return three ? launch_march_one<R, RECON, JX_HLLE, 3>(p, grid, s) : launch_march_one<R, RECON, JX_HLLE, 4>(p, grid, s);
-    case JX_ROE: return three ? launch_march_one<R, RECON, JX_ROE, 3>(p, grid, s) : launch_march_one<R, RECON, JX_ROE, 4>(p, grid, s);
-  }
-  return cudaErrorInvalidValue;
-}
-
-template <typename R, int RECON, int NV, int NC>
-cudaError_t launch_batch_march_nc(int rsolver, const StageParams* params, const int* offsets, int nsolves, int nwork,
-                                  dim3 grid, cudaStream_t s) {
-  constexpr int T = kMarchWarps * 32;
-  switch (rsolver) {
-    case JX_LLF: stage_kernel_batch_march<R, RECON, JX_LLF, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
-    case JX_HLLE: stage_kernel_batch_march<R, RECON, JX_HLLE, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
-    case JX_ROE: stage_kernel_batch_march<R, RECON, JX_ROE, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-template <typename R, int RECON, int NV>
-cudaError_t launch_batch_march_nv(int rsolver, int nc, const StageParams* params, const int* offsets, int nsolves,
-                                  int nwork, dim3 grid, cudaStream_t s) {
-  if constexpr (sizeof(R) == 4) {
-    if (nc == 1) return launch_batch_march_nc<R, RECON, NV, 1>(rsolver, params, offsets, nsolves, nwork, grid, s);
-    if (nc == 3) return launch_batch_march_nc<R, RECON, NV, 3>(rsolver, params, offsets, nsolves, nwork, grid, s);
-  }
-  if (nc != 2) return cudaErrorInvalidValue;
-  return launch_batch_march_nc<R, RECON, NV, 2>(rsolver, params, offsets, nsolves, nwork, grid, s);
-}
-
-template <typename R, int RECON>
-cudaError_t launch_batch_march_typed(int rsolver, int nv, int nc, const StageParams* params, const int* offsets,
-                                     int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  return nv == 3 ? launch_batch_march_nv<R, RECON, 3>(rsolver, nc, params, offsets, nsolves, nwork, grid, s)
-                 : launch_batch_march_nv<R, RECON, 4>(rsolver, nc, params, offsets, nsolves, nwork, grid, s);
-}
-
 }  // namespace jx
 
 namespace jx {
 
-template <int RECON>
-cudaError_t launch_march_recon(int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
-  if (dtype == JX_F64) return launch_march_typed<double, RECON>(rsolver, p, grid, s);
-  return launch_march_typed<float, RECON>(rsolver, p, grid, s);
+// Entry points for one (reconstruction, Riemann solver): each march_*.cu
+// translation unit instantiates one pair, so the build compiles the kernels
+// in parallel.
+template <int RECON, int RS>
+cudaError_t launch_march_rs(int dtype, const StageParams& p, dim3 grid, cudaStream_t s) {
+  const bool three = p.nv == 3;
+  if (dtype == JX_F64)
+    return three ? launch_march_one<double, RECON, RS, 3>(p, grid, s) : launch_march_one<double, RECON, RS, 4>(p, grid, s);
+  return three ? launch_march_one<float, RECON, RS, 3>(p, grid, s) : launch_march_one<float, RECON, RS, 4>(p, grid, s);
 }
 
-template <int RECON>
-cudaError_t launch_batch_march_recon(int dtype, int rsolver, int nv, int nc, const StageParams* params,
-                                     const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+template <typename R, int RECON, int RS, int NV>
+cudaError_t launch_batch_march_rs_nv(int nc, const StageParams* params, const int* offsets, int nsolves, int nwork,
+                                     dim3 grid, cudaStream_t s) {
+  constexpr int T = kMarchWarps * 32;
+  if constexpr (sizeof(R) == 4) {
+    if (nc == 1) {
+      stage_kernel_batch_march<R, RECON, RS, NV, 1><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
+      return cudaGetLastError();
+    }
+    if (nc == 3) {
+      stage_kernel_batch_march<R, RECON, RS, NV, 3><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
+      return cudaGetLastError();
+    }
+  }
+  if (nc != 2) return cudaErrorInvalidValue;
+  stage_kernel_batch_march<R, RECON, RS, NV, 2><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
+  return cudaGetLastError();
+}
+
+template <int RECON, int RS>
+cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+                                  int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   if (dtype == JX_F64)
-    return launch_batch_march_typed<double, RECON>(rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
-  return launch_batch_march_typed<float, RECON>(rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    return nv == 3 ? launch_batch_march_rs_nv<double, RECON, RS, 3>(nc, params, offsets, nsolves, nwork, grid, s)
+                   : launch_batch_march_rs_nv<double, RECON, RS, 4>(nc, params, offsets, nsolves, nwork, grid, s);
+  return nv == 3 ? launch_batch_march_rs_nv<float, RECON, RS, 3>(nc, params, offsets, nsolves, nwork, grid, s)
+                 : launch_batch_march_rs_nv<float, RECON, RS, 4>(nc, params, offsets, nsolves, nwork, grid, s);
 }
 
 template <typename Kernel>
-int march_occupancy(Kernel kernel) {
+int march_occupancy(Kernel kernel, size_t smem = 0) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kMarchWarps * 32, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kMarchWarps * 32, smem) != cudaSuccess) return 0;
   return n;
 }
 
@@ -585,6 +691,16 @@ int march_blocks_per_sm_nc(int nv, bool batch) {
   if (batch)
     return nv == 3 ? march_occupancy(stage_kernel_batch_march<R, RECON, RS, 3, NC>)
                    : march_occupancy(stage_kernel_batch_march<R, RECON, RS, 4, NC>);
+  // Float32 tiles of the automatic heights may run the ring kernel: count
+  // the blocks that fit with its shared memory (the register path fits as many).
+  if constexpr (sizeof(R) == 4) {
+    if (nv == 3) {
+      march_prefer_shared<stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric, true>>();
+      return march_occupancy(stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric, true>, march_smem<NC>());
+    }
+    march_prefer_shared<stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric, true>>();
+    return march_occupancy(stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric, true>, march_smem<NC>());
+  }
   return nv == 3 ? march_occupancy(stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric>)
                  : march_occupancy(stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric>);
 }
@@ -598,16 +714,10 @@ int march_blocks_per_sm_rs(int nv, int nc, bool batch) {
   return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, batch) : 0;
 }
 
-template <int RECON>
-int march_blocks_per_sm_recon(int dtype, int rsolver, int nv, int nc, bool batch) {
-  if (dtype == JX_F64) {
-    if (rsolver == JX_LLF) return march_blocks_per_sm_rs<double, RECON, JX_LLF>(nv, nc, batch);
-    if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<double, RECON, JX_HLLE>(nv, nc, batch);
-    return march_blocks_per_sm_rs<double, RECON, JX_ROE>(nv, nc, batch);
-  }
-  if (rsolver == JX_LLF) return march_blocks_per_sm_rs<float, RECON, JX_LLF>(nv, nc, batch);
-  if (rsolver == JX_HLLE) return march_blocks_per_sm_rs<float, RECON, JX_HLLE>(nv, nc, batch);
-  return march_blocks_per_sm_rs<float, RECON, JX_ROE>(nv, nc, batch);
+template <int RECON, int RS>
+int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, bool batch) {
+  return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, batch)
+                         : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, batch);
 }
 
 }  // namespace jx

@@ -1,16 +1,45 @@
-// Register-marching stage-kernel instantiations for the dc reconstruction
-// (float64 and float32, all three Riemann solvers, 3 or 4 variables).
-#include "jx_stage_march.cuh"
+// Register-marching stage kernels for the dc reconstruction: dispatch by
+// Riemann solver to the march_dc_<solver>.cu translation units, which
+// hold the instantiations (one per solver, so the build compiles them in
+// parallel).
+#include "jx_internal.h"
 
 namespace jx {
+cudaError_t launch_march_dc_llf(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
+cudaError_t launch_batch_march_dc_llf(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+                                  int nsolves, int nwork, dim3 grid, cudaStream_t s);
+int march_blocks_per_sm_dc_llf(int dtype, int nv, int nc, bool batch);
+cudaError_t launch_march_dc_hlle(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
+cudaError_t launch_batch_march_dc_hlle(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+                                  int nsolves, int nwork, dim3 grid, cudaStream_t s);
+int march_blocks_per_sm_dc_hlle(int dtype, int nv, int nc, bool batch);
+cudaError_t launch_march_dc_roe(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
+cudaError_t launch_batch_march_dc_roe(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+                                  int nsolves, int nwork, dim3 grid, cudaStream_t s);
+int march_blocks_per_sm_dc_roe(int dtype, int nv, int nc, bool batch);
+
 cudaError_t launch_march_dc(int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
-  return launch_march_recon<JX_DC>(dtype, rsolver, p, grid, s);
+  switch (rsolver) {
+    case JX_LLF: return launch_march_dc_llf(dtype, p, grid, s);
+    case JX_HLLE: return launch_march_dc_hlle(dtype, p, grid, s);
+    case JX_ROE: return launch_march_dc_roe(dtype, p, grid, s);
+  }
+  return cudaErrorInvalidValue;
 }
 cudaError_t launch_batch_march_dc(int dtype, int rsolver, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  return launch_batch_march_recon<JX_DC>(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+  switch (rsolver) {
+    case JX_LLF: return launch_batch_march_dc_llf(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_HLLE: return launch_batch_march_dc_hlle(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_ROE: return launch_batch_march_dc_roe(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
+  }
+  return cudaErrorInvalidValue;
 }
 int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch) {
-  return march_blocks_per_sm_recon<JX_DC>(dtype, rsolver, nv, nc, batch);
+  switch (rsolver) {
+    case JX_LLF: return march_blocks_per_sm_dc_llf(dtype, nv, nc, batch);
+    case JX_HLLE: return march_blocks_per_sm_dc_hlle(dtype, nv, nc, batch);
+    default: return march_blocks_per_sm_dc_roe(dtype, nv, nc, batch);
+  }
 }
 }  // namespace jx

@@ -1,0 +1,16 @@
+// Register-marching stage-kernel instantiations for the ppmx reconstruction
+// with the llf Riemann solver (float64 and float32, 3 or 4 variables).
+#include "jx_stage_march.cuh"
+
+namespace jx {
+cudaError_t launch_march_ppmx_llf(int dtype, const StageParams& p, dim3 grid, cudaStream_t s) {
+  return launch_march_rs<JX_PPMX, JX_LLF>(dtype, p, grid, s);
+}
+cudaError_t launch_batch_march_ppmx_llf(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+                                  int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+  return launch_batch_march_rs<JX_PPMX, JX_LLF>(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
+}
+int march_blocks_per_sm_ppmx_llf(int dtype, int nv, int nc, bool batch) {
+  return march_blocks_per_sm_rs_dtype<JX_PPMX, JX_LLF>(dtype, nv, nc, batch);
+}
+}  // namespace jx
