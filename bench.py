@@ -42,7 +42,7 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # profiles/; None until such a capture exists for the dtype.
 # DRAM bytes (read + write) of one RK3 stage-2 launch at 4096^2, from a one-pass
 # ncu capture of this benchmark (dram__bytes_read.sum + dram__bytes_write.sum).
-STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (607.19e6 + 240.69e6) / 4096**2}
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (552.06e6 + 236.47e6) / 4096**2}
 
 
 def parse_args():

@@ -52,10 +52,11 @@ typedef struct {
   int32_t dtype;          /* jx_dtype */
   int32_t recon, rsolver, integrator;
   /* Stage tile. 0, 0 = library default: for 3/4 variables, float32 uses
-   * the register-marching kernel (58 x h tiles, h chosen per device) and
-   * float64 32 x 16 shared-memory tiles. tile_x = 58 selects marching
-   * tiles for 3/4 variables (tile_y >= 8 rows, or 0 for automatic). Any
-   * other tile_x x tile_y is a shared-memory tile. See jx_tile_info. */
+   * the register-marching kernel (58 x h tiles, 26 x h for WENO-Z, h
+   * chosen per device and grid) and float64 32 x 16 shared-memory tiles.
+   * tile_x = 26, 58 or 90 selects marching tiles for 3/4 variables
+   * (tile_y >= 8 rows, or 0 for automatic). Any other tile_x x tile_y is a
+   * shared-memory tile. See jx_tile_info. */
   int32_t tile_x, tile_y;
   double dx, dy, cs, dfloor;
   double viscosity, smagorinsky_cs, drag_rate;

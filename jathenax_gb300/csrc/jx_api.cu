@@ -97,19 +97,23 @@ int sm_count();
 
 // Resident marching blocks per SM for this descriptor on the current device
 // (cached; 4 when the device cannot be queried).
+// Resident marching blocks per SM for a descriptor's solve: the kernel its
+// stages run (the lean form for an inviscid problem without drag, whose
+// register count, and so occupancy, can differ from the generic form's).
 int march_occupancy(const jx_desc* d, int nc) {
-  static int cache[64][2][5][3][2][3];
+  static int cache[64][2][5][3][2][3][2];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 4;
-  int& c = cache[dev][d->dtype][d->recon][d->rsolver][d->nvar - 3][nc - 1];
+  const bool lean = d->viscosity == 0.0 && d->smagorinsky_cs == 0.0 && d->drag_rate == 0.0;
+  int& c = cache[dev][d->dtype][d->recon][d->rsolver][d->nvar - 3][nc - 1][lean];
   if (c == 0) {
     int n = 0;
     switch (d->recon) {
-      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, nc, false); break;
-      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, nc, false); break;
-      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, nc, false); break;
-      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, nc, false); break;
-      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, nc, false); break;
+      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
+      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
+      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
+      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
+      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
     }
     if (n < 1) {
       cudaGetLastError();
@@ -155,14 +159,16 @@ int march_rows(const jx_desc* d, int nc) {
 }
 
 jx_status resolve_tile(const jx_desc* d, Tile* t, bool device = true) {
-  // Automatic tiles: float32 marches with two columns per lane; float64,
-  // bound by the FP64 pipe, keeps the shared-memory tile, which evaluates no
-  // halo faces twice. An explicit tile width of 26, 58 or 90 asks for the
-  // marching kernel with 1, 2 or 3 columns per lane (float64: 58 only).
+  // Automatic tiles: float32 marches with two columns per lane (WENO-Z,
+  // whose long stencil needs the registers, with one: 1.36 against 1.48 ms
+  // per 4096² stage at the best heights); float64, bound by the FP64 pipe,
+  // keeps the shared-memory tile, which evaluates no halo faces twice. An
+  // explicit tile width of 26, 58 or 90 asks for the marching kernel with
+  // 1, 2 or 3 columns per lane (float64: 58 only).
   const bool three_four = d->nvar == 3 || d->nvar == 4;
   const int want_nc = march_cols(d->tile_x);
   const bool march = three_four && (want_nc > 0 || (d->tile_x == 0 && d->tile_y == 0 && d->dtype == JX_F32));
-  const int nc = want_nc > 0 ? want_nc : 2;
+  const int nc = want_nc > 0 ? want_nc : (d->dtype == JX_F32 && d->recon == JX_WENOZ ? 1 : 2);
   if (march && d->dtype == JX_F64 && nc != 2)
     return fail(JX_ERR_INVALID, "float64 marching tiles are %d columns wide, not %d", kMarchTileX, d->tile_x);
   int tx = d->tile_x > 0 && !march ? d->tile_x : 32;
@@ -812,11 +818,11 @@ cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* p
 
 int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc) {
   switch (recon) {
-    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, true);
-    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, true);
-    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, true);
-    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, true);
-    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, true);
+    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, true, false);
+    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, true, false);
+    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, true, false);
+    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, true, false);
+    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, true, false);
   }
 }
 

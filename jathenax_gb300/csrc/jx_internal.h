@@ -141,11 +141,11 @@ cudaError_t launch_batch_march_plm(int, int, int, int, const StageParams*, const
 cudaError_t launch_batch_march_ppm4(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
 cudaError_t launch_batch_march_ppmx(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
 cudaError_t launch_batch_march_wenoz(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch);
-int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch);
-int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, bool batch);
-int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, int nc, bool batch);
-int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, int nc, bool batch);
+int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
+int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
+int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
+int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
+int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
 
 typedef cudaError_t (*FaceStatesLauncher)(int dtype, const void* W, int ny, int nx, int nv,
                                           int axis, double dfloor, void* left, void* right,

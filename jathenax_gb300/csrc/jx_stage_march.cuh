@@ -163,6 +163,13 @@ __device__ __forceinline__ void lane_cells(const Cell4<R> (&own)[NC], Cell4<R> (
 // was 7 % slower (0.027 -> 0.029 ms), so tiles shorter than kRingMinRows
 // keep the register path. The bits are the same either way.
 constexpr int kRingU = 8, kRingV = 4, kRingAhead = 3, kRingMinRows = 24;
+// Where the ring is built: float32, not DC (nearest to the HBM bound, 0.175
+// ms per 4096² stage on the register path against 0.193 with the ring) and
+// not WENO-Z with two or three columns per lane (58 x 121: 1.478 against
+// 1.506 ms); PLM, PPM4, PPMX and one-column WENO-Z gain 1-22 %.
+template <typename R, int RECON, int NC> constexpr bool march_ring_on() {
+  return sizeof(R) == 4 && RECON != JX_DC && (RECON != JX_WENOZ || NC == 1);
+}
 template <int NC> __host__ __device__ constexpr int march_ring_bytes() { return (kRingU + kRingV) * NC * 32 * 16; }
 
 __device__ __forceinline__ void cp_async_16(void* smem, const void* gmem) {
@@ -600,7 +607,7 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // choice for small grids) runs the generic form.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
-  if constexpr (sizeof(R) == 4) {
+  if constexpr (march_ring_on<R, RECON, NC>()) {
     if (p.ty >= kRingMinRows) {
       march_prefer_shared<stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>>();
       stage_kernel_march<R, RECON, RS, NV, NC, FORM, true><<<blocks, threads, march_smem<NC>(), s>>>(p, ntiles);
@@ -686,38 +693,47 @@ int march_occupancy(Kernel kernel, size_t smem = 0) {
 }
 
 // Resident marching blocks per SM (single-solve or batch kernel).
-template <typename R, int RECON, int RS, int NC>
-int march_blocks_per_sm_nc(int nv, bool batch) {
-  if (batch)
-    return nv == 3 ? march_occupancy(stage_kernel_batch_march<R, RECON, RS, 3, NC>)
-                   : march_occupancy(stage_kernel_batch_march<R, RECON, RS, 4, NC>);
-  // Float32 tiles of the automatic heights may run the ring kernel: count
-  // the blocks that fit with its shared memory (the register path fits as many).
-  if constexpr (sizeof(R) == 4) {
-    if (nv == 3) {
-      march_prefer_shared<stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric, true>>();
-      return march_occupancy(stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric, true>, march_smem<NC>());
-    }
-    march_prefer_shared<stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric, true>>();
-    return march_occupancy(stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric, true>, march_smem<NC>());
+// Resident blocks per SM of the kernel a launch would run: the batch
+// kernel, or the single-solve kernel in its lean blend form (float32, two or
+// three columns per lane, an inviscid problem without drag) or its generic
+// form, with the ring's shared memory where the ring is built.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM>
+int march_single_occupancy() {
+  constexpr bool ring = march_ring_on<R, RECON, NC>();
+  if constexpr (ring) {
+    march_prefer_shared<stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>>();
+    return march_occupancy(stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>, march_smem<NC>());
   }
-  return nv == 3 ? march_occupancy(stage_kernel_march<R, RECON, RS, 3, NC, kMarchGeneric>)
-                 : march_occupancy(stage_kernel_march<R, RECON, RS, 4, NC, kMarchGeneric>);
+  return march_occupancy(stage_kernel_march<R, RECON, RS, NV, NC, FORM>);
+}
+
+template <typename R, int RECON, int RS, int NV, int NC>
+int march_blocks_per_sm_nv(bool batch, bool lean) {
+  if (batch) return march_occupancy(stage_kernel_batch_march<R, RECON, RS, NV, NC>);
+  if constexpr (sizeof(R) == 4 && NC > 1)
+    if (lean) return march_single_occupancy<R, RECON, RS, NV, NC, kMarchLeanBlend>();
+  return march_single_occupancy<R, RECON, RS, NV, NC, kMarchGeneric>();
+}
+
+template <typename R, int RECON, int RS, int NC>
+int march_blocks_per_sm_nc(int nv, bool batch, bool lean) {
+  return nv == 3 ? march_blocks_per_sm_nv<R, RECON, RS, 3, NC>(batch, lean)
+                 : march_blocks_per_sm_nv<R, RECON, RS, 4, NC>(batch, lean);
 }
 
 template <typename R, int RECON, int RS>
-int march_blocks_per_sm_rs(int nv, int nc, bool batch) {
+int march_blocks_per_sm_rs(int nv, int nc, bool batch, bool lean) {
   if constexpr (sizeof(R) == 4) {
-    if (nc == 1) return march_blocks_per_sm_nc<R, RECON, RS, 1>(nv, batch);
-    if (nc == 3) return march_blocks_per_sm_nc<R, RECON, RS, 3>(nv, batch);
+    if (nc == 1) return march_blocks_per_sm_nc<R, RECON, RS, 1>(nv, batch, lean);
+    if (nc == 3) return march_blocks_per_sm_nc<R, RECON, RS, 3>(nv, batch, lean);
   }
-  return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, batch) : 0;
+  return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, batch, lean) : 0;
 }
 
 template <int RECON, int RS>
-int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, bool batch) {
-  return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, batch)
-                         : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, batch);
+int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, bool batch, bool lean) {
+  return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, batch, lean)
+                         : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, batch, lean);
 }
 
 }  // namespace jx

@@ -8,15 +8,15 @@ namespace jx {
 cudaError_t launch_march_dc_llf(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_dc_llf(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_dc_llf(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_dc_llf(int dtype, int nv, int nc, bool batch, bool lean);
 cudaError_t launch_march_dc_hlle(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_dc_hlle(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_dc_hlle(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_dc_hlle(int dtype, int nv, int nc, bool batch, bool lean);
 cudaError_t launch_march_dc_roe(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_dc_roe(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_dc_roe(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_dc_roe(int dtype, int nv, int nc, bool batch, bool lean);
 
 cudaError_t launch_march_dc(int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
   switch (rsolver) {
@@ -35,11 +35,11 @@ cudaError_t launch_batch_march_dc(int dtype, int rsolver, int nv, int nc, const 
   }
   return cudaErrorInvalidValue;
 }
-int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch) {
+int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch, bool lean) {
   switch (rsolver) {
-    case JX_LLF: return march_blocks_per_sm_dc_llf(dtype, nv, nc, batch);
-    case JX_HLLE: return march_blocks_per_sm_dc_hlle(dtype, nv, nc, batch);
-    default: return march_blocks_per_sm_dc_roe(dtype, nv, nc, batch);
+    case JX_LLF: return march_blocks_per_sm_dc_llf(dtype, nv, nc, batch, lean);
+    case JX_HLLE: return march_blocks_per_sm_dc_hlle(dtype, nv, nc, batch, lean);
+    default: return march_blocks_per_sm_dc_roe(dtype, nv, nc, batch, lean);
   }
 }
 }  // namespace jx

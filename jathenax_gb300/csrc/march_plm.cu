@@ -8,15 +8,15 @@ namespace jx {
 cudaError_t launch_march_plm_llf(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_plm_llf(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_plm_llf(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_plm_llf(int dtype, int nv, int nc, bool batch, bool lean);
 cudaError_t launch_march_plm_hlle(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_plm_hlle(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_plm_hlle(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_plm_hlle(int dtype, int nv, int nc, bool batch, bool lean);
 cudaError_t launch_march_plm_roe(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
 cudaError_t launch_batch_march_plm_roe(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
-int march_blocks_per_sm_plm_roe(int dtype, int nv, int nc, bool batch);
+int march_blocks_per_sm_plm_roe(int dtype, int nv, int nc, bool batch, bool lean);
 
 cudaError_t launch_march_plm(int dtype, int rsolver, const StageParams& p, dim3 grid, cudaStream_t s) {
   switch (rsolver) {
@@ -35,11 +35,11 @@ cudaError_t launch_batch_march_plm(int dtype, int rsolver, int nv, int nc, const
   }
   return cudaErrorInvalidValue;
 }
-int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch) {
+int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch, bool lean) {
   switch (rsolver) {
-    case JX_LLF: return march_blocks_per_sm_plm_llf(dtype, nv, nc, batch);
-    case JX_HLLE: return march_blocks_per_sm_plm_hlle(dtype, nv, nc, batch);
-    default: return march_blocks_per_sm_plm_roe(dtype, nv, nc, batch);
+    case JX_LLF: return march_blocks_per_sm_plm_llf(dtype, nv, nc, batch, lean);
+    case JX_HLLE: return march_blocks_per_sm_plm_hlle(dtype, nv, nc, batch, lean);
+    default: return march_blocks_per_sm_plm_roe(dtype, nv, nc, batch, lean);
   }
 }
 }  // namespace jx

@@ -10,7 +10,7 @@ cudaError_t launch_batch_march_ppm4_roe(int dtype, int nv, int nc, const StagePa
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   return launch_batch_march_rs<JX_PPM4, JX_ROE>(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
 }
-int march_blocks_per_sm_ppm4_roe(int dtype, int nv, int nc, bool batch) {
-  return march_blocks_per_sm_rs_dtype<JX_PPM4, JX_ROE>(dtype, nv, nc, batch);
+int march_blocks_per_sm_ppm4_roe(int dtype, int nv, int nc, bool batch, bool lean) {
+  return march_blocks_per_sm_rs_dtype<JX_PPM4, JX_ROE>(dtype, nv, nc, batch, lean);
 }
 }  // namespace jx

@@ -10,7 +10,7 @@ cudaError_t launch_batch_march_wenoz_llf(int dtype, int nv, int nc, const StageP
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   return launch_batch_march_rs<JX_WENOZ, JX_LLF>(dtype, nv, nc, params, offsets, nsolves, nwork, grid, s);
 }
-int march_blocks_per_sm_wenoz_llf(int dtype, int nv, int nc, bool batch) {
-  return march_blocks_per_sm_rs_dtype<JX_WENOZ, JX_LLF>(dtype, nv, nc, batch);
+int march_blocks_per_sm_wenoz_llf(int dtype, int nv, int nc, bool batch, bool lean) {
+  return march_blocks_per_sm_rs_dtype<JX_WENOZ, JX_LLF>(dtype, nv, nc, batch, lean);
 }
 }  // namespace jx
