@@ -450,9 +450,11 @@ def summary(line):
                               v["arrival_bound"]]
                           for k, v in sv.items() if isinstance(v, dict) and "solves_per_s" in v}
         out["serving_fields"] = ["solves_per_s", "speedup_vs_serial_fp64", "p50_s", "p99_s", "arrival_bound"]
-        errs = [v["fp32_l1_density_err_vs_fp64_max"] for v in sv.values()
-                if isinstance(v, dict) and v.get("fp32_l1_density_err_vs_fp64_max") is not None]
-        out["serving_fp32_l1_max"] = max(errs) if errs else None
+        for suffix, guarded in (("", True), ("_unguarded", False)):
+            errs = [v["fp32_l1_density_err_vs_fp64_max"] for k, v in sv.items()
+                    if isinstance(v, dict) and v.get("fp32_l1_density_err_vs_fp64_max") is not None
+                    and ("unguarded" not in k) == guarded]
+            out["serving_fp32_l1_max" + suffix] = max(errs) if errs else None
     p = line.get("precision")
     if p:
         out["precision_l1_density"] = {k: v["l1_density"] for k, v in p.items()}
@@ -547,9 +549,10 @@ def bench_serving(torch, n):
            "smooth/kh/turbulence, random recon/rsolver, 150 GB budget",
            "serial_fp64_solves_per_s": round(serial["solves_per_s"], 3)}
     for rate in (200.0, 1000.0):
-        for label, dtype in (("mixed_80pct_fp32", None), ("all_fp32", "float32")):
+        for label, dtype, guard in (("mixed_80pct_fp32", None, True), ("all_fp32", "float32", True),
+                                    ("all_fp32_unguarded", "float32", False)):
             reqs = stream(rate)
-            server = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype)
+            server = Server(budget_bytes=150e9, steps_per_tick=8, keep_results=True, dtype=dtype, guard=guard)
             server.warmup()
             stats = server.run(reqs)
             errs = [float(relative_l1(q.result, r.result)[0]) for r, q in zip(ref, reqs)
