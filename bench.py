@@ -42,6 +42,9 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # profiles/; None until such a capture exists for the dtype.
 # DRAM bytes (read + write) of one RK3 stage-2 launch at 4096^2, from a one-pass
 # ncu capture of this benchmark (dram__bytes_read.sum + dram__bytes_write.sum).
+# Thread instructions per cell of the float32 marching stage (ppm4+roe, 4
+# variables, row ring): smsp__inst_executed.sum x 32 / cells of one launch.
+STAGE_INST_PER_CELL_F32 = 146.83e6 * 32 / 3072**2
 STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (552.06e6 + 236.47e6) / 4096**2}
 
 
@@ -375,7 +378,7 @@ def bench_ours(args, world, rank, local):
         compute_frac = flops / peak_tflops
         hbm_frac = gbs / hbm_peak
         bound = "fp64" if key == "f64" else ("fp32" if compute_frac >= hbm_frac else "hbm")
-        family = "stage_kernel_march" if res["tile"][0] == 58 else "stage_kernel_fast"
+        family = "stage_kernel_march" if res["tile"][0] in (26, 58, 90) else "stage_kernel_fast"
         out = {"kernel": f"{family}<{'double' if w == 8 else 'float'},ppm4,roe,4> (RK3 stage 2, "
                          f"tile {res['tile'][0]}x{res['tile'][1]})",
                "bound": bound, "achieved": round(flops, 4), "peak": round(peak_tflops, 4),
@@ -396,6 +399,16 @@ def bench_ours(args, world, rank, local):
                 nominal = 2 * 2 * probe["sms"] * mhz * 1e6 / 1e12
                 out["fp64_nominal"] = {"peak": round(nominal, 4), "unit": "TFLOP/s", "frac": round(flops / nominal, 4),
                                        "peak_source": f"2 DFMA/SM/clk x {probe['sms']} SMs x {mhz:.0f} MHz"}
+        if key == "f32":
+            # The float32 marching stage is bound by instruction issue: its
+            # executed instructions per cell (ncu, 3072² case) over the issue
+            # rate of every scheduler (4 per SM, one warp instruction per clock).
+            mhz = (res.get("clocks") or {}).get("sm_mhz") or probe["sm_mhz"]
+            if mhz:
+                bound_ms = cells * STAGE_INST_PER_CELL_F32 / 32 / (probe["sms"] * 4 * mhz * 1e6) * 1e3
+                out["issue"] = {"thread_instructions_per_cell": round(STAGE_INST_PER_CELL_F32, 1), "bound_ms": round(bound_ms, 4),
+                                "frac": round(bound_ms / res["stage_ms"], 4),
+                                "source": "smsp__inst_executed.sum of one stage launch (ncu, 3072x3072)"}
         if bound == "hbm":
             out.update(achieved=round(gbs, 1), peak=hbm_peak, unit="GB/s", frac=round(hbm_frac, 4),
                        peak_source=f"hbm_gbs of {peak_kind}")

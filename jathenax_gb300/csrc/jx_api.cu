@@ -109,11 +109,11 @@ int march_occupancy(const jx_desc* d, int nc) {
   if (c == 0) {
     int n = 0;
     switch (d->recon) {
-      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
-      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
-      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
-      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
-      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, nc, false, lean); break;
+      case JX_DC: n = march_blocks_per_sm_dc(d->dtype, d->rsolver, d->nvar, nc, lean ? kMarchSingleLean : kMarchSingle); break;
+      case JX_PLM: n = march_blocks_per_sm_plm(d->dtype, d->rsolver, d->nvar, nc, lean ? kMarchSingleLean : kMarchSingle); break;
+      case JX_PPM4: n = march_blocks_per_sm_ppm4(d->dtype, d->rsolver, d->nvar, nc, lean ? kMarchSingleLean : kMarchSingle); break;
+      case JX_PPMX: n = march_blocks_per_sm_ppmx(d->dtype, d->rsolver, d->nvar, nc, lean ? kMarchSingleLean : kMarchSingle); break;
+      default: n = march_blocks_per_sm_wenoz(d->dtype, d->rsolver, d->nvar, nc, lean ? kMarchSingleLean : kMarchSingle); break;
     }
     if (n < 1) {
       cudaGetLastError();
@@ -722,14 +722,16 @@ jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, 
 namespace {
 
 constexpr uint32_t kPlanMagic = 0x4a584250;  // "JXBP"
-// 2 precisions x 5 reconstructions x 3 solvers x 7 kernel classes (shared
-// memory; marching with 3 or 4 variables at 1, 2 or 3 columns per lane)
-constexpr int kMaxGroups = 210;
+// 2 precisions x 5 reconstructions x 3 solvers x 13 kernel classes (shared
+// memory; marching with 3 or 4 variables at 1, 2 or 3 columns per lane, with
+// or without the row ring)
+constexpr int kMaxGroups = 390;
 
 struct BatchGroup {
   int dtype, recon, rsolver, first, count, tile_first, nwork, march;
   int nv;   // marching groups: the variable count of every solve (0 in shared-memory groups)
   int nc;   // marching groups: columns per lane (0 in shared-memory groups)
+  int ring;  // marching groups: the row-ring kernel runs (member tiles of kRingMinRows rows or more)
   int bps;  // resident blocks per SM of the group's kernel (occupancy at plan time)
   size_t smem;
 };
@@ -816,24 +818,24 @@ cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* p
   }
 }
 
-int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc) {
+int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc, int ring) {
   switch (recon) {
-    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, true, false);
-    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, true, false);
-    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, true, false);
-    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, true, false);
-    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, true, false);
+    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
+    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
+    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
+    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
+    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
   }
 }
 
-cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, int nc, const StageParams* params,
+cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, int nc, int ring, const StageParams* params,
                                const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   switch (recon) {
-    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
-    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
-    default: return launch_batch_march_wenoz(dtype, rsolver, nv, nc, params, offsets, nsolves, nwork, grid, s);
+    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    default: return launch_batch_march_wenoz(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
   }
 }
 
@@ -940,10 +942,11 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
     const int march = tl[i].march ? 1 : 0;
     const int nv = march ? d.nvar : 0;
     const int nc = march ? tl[i].mnc : 0;
+    const int ring = march && march_ring_built(d.dtype == JX_F32, d.recon, nc) && tl[i].mty >= kRingMinRows;
     int g = 0;
     while (g < n_groups && !(h->groups[g].dtype == d.dtype && h->groups[g].recon == d.recon &&
                              h->groups[g].rsolver == d.rsolver && h->groups[g].march == march &&
-                             h->groups[g].nv == nv && h->groups[g].nc == nc))
+                             h->groups[g].nv == nv && h->groups[g].nc == nc && h->groups[g].ring == ring))
       ++g;
     if (g == n_groups) {
       if (n_groups == kMaxGroups) return fail(JX_ERR_INVALID, "more than %d solver groups", kMaxGroups);
@@ -954,6 +957,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
       G.march = march;
       G.nv = nv;
       G.nc = nc;
+      G.ring = ring;
       G.smem = 0;
     }
     if (!march && tl[i].fast_smem > h->groups[g].smem) h->groups[g].smem = tl[i].fast_smem;
@@ -1015,7 +1019,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
   h->n_groups = n_groups;
   for (int g = 0; g < n_groups; ++g) {
     BatchGroup& G = h->groups[g];
-    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv, G.nc)
+    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring)
                     : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
     if (G.bps < 1) {
       cudaGetLastError();  // no device to query: one block per SM
@@ -1118,7 +1122,7 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
       const int* offs = offsets_dev + G.tile_first;
       cudaStream_t gs = side ? side->s[g % kSideStreams] : s;
       const cudaError_t e =
-          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, G.nc, P, offs, G.count, G.nwork,
+          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring, P, offs, G.count, G.nwork,
                                        dim3((unsigned)blocks), gs)
                   : launch_batch(G.recon, G.dtype, G.rsolver, P, offs, G.count, G.nwork, dim3((unsigned)blocks),
                                  G.smem, gs);

@@ -123,6 +123,16 @@ constexpr int kMarchWarps = 1;
 __host__ __device__ constexpr int march_tile_x(int nc) { return 32 * nc - 6; }
 constexpr int kMarchTileX = march_tile_x(2);
 constexpr int kMarchMinRows = 8;
+// Float32 marching kernels stage a tile's rows in a shared-memory ring (see
+// jx_stage_march.cuh) on tiles of at least kRingMinRows rows, for the
+// reconstructions and column counts where that measured faster: not DC, and
+// WENO-Z with one column per lane only.
+constexpr int kRingMinRows = 24;
+__host__ __device__ constexpr bool march_ring_built(bool f32, int recon, int nc) {
+  return f32 && recon != JX_DC && (recon != JX_WENOZ || nc == 1);
+}
+// Which marching kernel an occupancy query is for.
+enum MarchKind { kMarchSingle = 0, kMarchSingleLean = 1, kMarchBatch = 2, kMarchBatchRing = 3 };
 // Columns per lane of a marching tile width (0: not a marching width).
 inline int march_cols(int tile_x) {
   for (int nc = 1; nc <= 3; ++nc)
@@ -136,16 +146,16 @@ cudaError_t launch_march_ppm4(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_ppmx(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_wenoz(int, int, const StageParams&, dim3, cudaStream_t);
 // (dtype, rsolver, nv, nc, params, tile offsets, nsolves, nwork, grid, stream)
-cudaError_t launch_batch_march_dc(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_plm(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppm4(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppmx(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_wenoz(int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
-int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
-int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
-int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
-int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, int nc, bool batch, bool lean);
+cudaError_t launch_batch_march_dc(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_plm(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppm4(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppmx(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_wenoz(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, int kind);
+int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, int kind);
+int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, int kind);
+int march_blocks_per_sm_ppmx(int dtype, int rsolver, int nv, int nc, int kind);
+int march_blocks_per_sm_wenoz(int dtype, int rsolver, int nv, int nc, int kind);
 
 typedef cudaError_t (*FaceStatesLauncher)(int dtype, const void* W, int ny, int nx, int nv,
                                           int axis, double dfloor, void* left, void* right,

@@ -26,6 +26,8 @@
 #include "jx_device.cuh"
 #include "jx_internal.h"
 #include "jx_stage_fast.cuh"
+#include "jx_ring.cuh"
+#include "jx_stage_march_pk.cuh"
 
 #include <utility>
 
@@ -151,62 +153,6 @@ __device__ __forceinline__ void lane_cells(const Cell4<R> (&own)[NC], Cell4<R> (
   lane_cells_impl<NC, R, NV>(own, E, std::make_integer_sequence<int, NC + 4>{});
 }
 
-// Row ring of the float32 single-solve walk on tall tiles: rows of U arrive
-// by cp.async three rows ahead of their use and rows of V three rows ahead
-// of the RK combine, into shared memory that only the copying lane reads
-// (slot [row][column h][lane], 16 bytes a cell, so a warp's accesses are
-// conflict-free). kRingU rows of U stay until the combine of the row has
-// read them too (its U then comes from the ring, not from L1/L2); kRingV
-// rows of V. No register holds a row in flight. Measured on GB300 at 4096²
-// (ppm4+roe, float32, RK3 stage 2): 0.2957 -> 0.2814 ms on 58 x 121 tiles,
-// 0.3144 -> 0.2792 ms on 90 x 106; on the 8-row tiles of a 1024² grid it
-// was 7 % slower (0.027 -> 0.029 ms), so tiles shorter than kRingMinRows
-// keep the register path. The bits are the same either way.
-constexpr int kRingU = 8, kRingV = 4, kRingAhead = 3, kRingMinRows = 24;
-// Where the ring is built: float32, not DC (nearest to the HBM bound, 0.175
-// ms per 4096² stage on the register path against 0.193 with the ring) and
-// not WENO-Z with two or three columns per lane (58 x 121: 1.478 against
-// 1.506 ms); PLM, PPM4, PPMX and one-column WENO-Z gain 1-22 %.
-template <typename R, int RECON, int NC> constexpr bool march_ring_on() {
-  return sizeof(R) == 4 && RECON != JX_DC && (RECON != JX_WENOZ || NC == 1);
-}
-template <int NC> __host__ __device__ constexpr int march_ring_bytes() { return (kRingU + kRingV) * NC * 32 * 16; }
-
-__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// One cell (NV floats) from global to its ring slot.
-template <int NV>
-__device__ __forceinline__ void ring_copy(float4* slot, const float* g) {
-  if constexpr (NV == 4) {
-    cp_async_16(slot, g);
-  } else {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) cp_async_4(reinterpret_cast<float*>(slot) + v, g + v);
-  }
-}
-
-template <int NV>
-__device__ __forceinline__ Cell4<float> ring_read(const float4* slot) {
-  const float4 t = *slot;
-  Cell4<float> c;
-  c.v[0] = t.x;
-  c.v[1] = t.y;
-  c.v[2] = t.z;
-  c.v[3] = NV == 4 ? t.w : 0.0f;
-  return c;
-}
 
 // PREFETCH_V: issue L2 prefetches of the saved register two rows ahead of
 // the RK combine. Measured on GB300: it helps the batch kernel (12 resident
@@ -568,6 +514,25 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, 
 
 template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
 
+// PPM4 + Roe with 4 variables in a lean form with two columns per lane runs
+// the packed-pair walk of jx_stage_march_pk.cuh (float32): 0.2812 -> 0.2642
+// ms per 4096² stage (58 x 121), 0.0269 -> 0.0249 ms at 1024²; with 3
+// variables it measured 1 % slower (0.2379 -> 0.2404 ms), so it keeps the
+// per-column walk.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
+  return sizeof(R) == 4 && RECON == JX_PPM4 && RS == JX_ROE && NV == 4 && NC == 2 && FORM != kMarchGeneric;
+}
+
+static_assert(kMarchWarps == 1, "the packed-pair kernel takes one tile per single-warp block");
+template <int NV, int FORM, bool RING>
+__global__ void __launch_bounds__(32, 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
+  if (p.clock->done) return;
+  const int tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  extern __shared__ float4 march_ring[];
+  pk::march_tile_pk<NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
+}
+
 // Let a ring kernel have the largest shared-memory carve-out (once per kernel).
 template <auto Kernel>
 void march_prefer_shared() {
@@ -583,7 +548,7 @@ void march_prefer_shared() {
 // warp takes work items round-robin; nothing is shared between warps. A
 // launch group holds solves of one variable count and one column count per
 // lane; each solve's stage options are read at run time.
-template <typename R, int RECON, int RS, int NV, int NC>
+template <typename R, int RECON, int RS, int NV, int NC, bool RING = false>
 __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, RECON, NC>())) stage_kernel_batch_march(
     const StageParams* __restrict__ params, const int* __restrict__ tile_offset, int nsolves, int nwork) {
   const int stride = gridDim.x * kMarchWarps;
@@ -597,7 +562,14 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
     const StageParams& p = params[lo];
     if (p.skip || p.clock->done) continue;
     const int tile = w - tile_offset[lo];
-    march_tile<R, RECON, RS, NV, NC, kMarchGeneric, true>(p, tile, tile_offset[lo + 1] - tile_offset[lo]);
+    if constexpr (RING && sizeof(R) == 4) {
+      // The ring is free again at the end of each tile (march_tile waits for its copies).
+      extern __shared__ float4 march_ring[];
+      march_tile<R, RECON, RS, NV, NC, kMarchGeneric, false, true>(
+          p, tile, tile_offset[lo + 1] - tile_offset[lo], march_ring + (threadIdx.x >> 5) * (march_ring_bytes<NC>() / 16));
+    } else {
+      march_tile<R, RECON, RS, NV, NC, kMarchGeneric, true>(p, tile, tile_offset[lo + 1] - tile_offset[lo]);
+    }
   }
 }
 
@@ -607,6 +579,15 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // choice for small grids) runs the generic form.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
+  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
+    if (p.ty >= kRingMinRows) {
+      march_prefer_shared<stage_kernel_march_pk<NV, FORM, true>>();
+      stage_kernel_march_pk<NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
+    } else {
+      stage_kernel_march_pk<NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
+    }
+    return cudaGetLastError();
+  }
   if constexpr (march_ring_on<R, RECON, NC>()) {
     if (p.ty >= kRingMinRows) {
       march_prefer_shared<stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>>();
@@ -656,33 +637,41 @@ cudaError_t launch_march_rs(int dtype, const StageParams& p, dim3 grid, cudaStre
   return three ? launch_march_one<float, RECON, RS, 3>(p, grid, s) : launch_march_one<float, RECON, RS, 4>(p, grid, s);
 }
 
-template <typename R, int RECON, int RS, int NV>
-cudaError_t launch_batch_march_rs_nv(int nc, const StageParams* params, const int* offsets, int nsolves, int nwork,
-                                     dim3 grid, cudaStream_t s) {
+template <typename R, int RECON, int RS, int NV, int NC>
+cudaError_t launch_batch_march_k(bool ring, const StageParams* params, const int* offsets, int nsolves, int nwork,
+                                 dim3 grid, cudaStream_t s) {
   constexpr int T = kMarchWarps * 32;
-  if constexpr (sizeof(R) == 4) {
-    if (nc == 1) {
-      stage_kernel_batch_march<R, RECON, RS, NV, 1><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
-      return cudaGetLastError();
-    }
-    if (nc == 3) {
-      stage_kernel_batch_march<R, RECON, RS, NV, 3><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
+  if constexpr (march_ring_on<R, RECON, NC>()) {
+    if (ring) {
+      march_prefer_shared<stage_kernel_batch_march<R, RECON, RS, NV, NC, true>>();
+      stage_kernel_batch_march<R, RECON, RS, NV, NC, true><<<grid, T, march_smem<NC>(), s>>>(params, offsets, nsolves,
+                                                                                            nwork);
       return cudaGetLastError();
     }
   }
-  if (nc != 2) return cudaErrorInvalidValue;
-  stage_kernel_batch_march<R, RECON, RS, NV, 2><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
+  stage_kernel_batch_march<R, RECON, RS, NV, NC><<<grid, T, 0, s>>>(params, offsets, nsolves, nwork);
   return cudaGetLastError();
 }
 
+template <typename R, int RECON, int RS, int NV>
+cudaError_t launch_batch_march_rs_nv(int nc, bool ring, const StageParams* params, const int* offsets, int nsolves,
+                                     int nwork, dim3 grid, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4) {
+    if (nc == 1) return launch_batch_march_k<R, RECON, RS, NV, 1>(ring, params, offsets, nsolves, nwork, grid, s);
+    if (nc == 3) return launch_batch_march_k<R, RECON, RS, NV, 3>(ring, params, offsets, nsolves, nwork, grid, s);
+  }
+  if (nc != 2) return cudaErrorInvalidValue;
+  return launch_batch_march_k<R, RECON, RS, NV, 2>(ring, params, offsets, nsolves, nwork, grid, s);
+}
+
 template <int RECON, int RS>
-cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   if (dtype == JX_F64)
-    return nv == 3 ? launch_batch_march_rs_nv<double, RECON, RS, 3>(nc, params, offsets, nsolves, nwork, grid, s)
-                   : launch_batch_march_rs_nv<double, RECON, RS, 4>(nc, params, offsets, nsolves, nwork, grid, s);
-  return nv == 3 ? launch_batch_march_rs_nv<float, RECON, RS, 3>(nc, params, offsets, nsolves, nwork, grid, s)
-                 : launch_batch_march_rs_nv<float, RECON, RS, 4>(nc, params, offsets, nsolves, nwork, grid, s);
+    return nv == 3 ? launch_batch_march_rs_nv<double, RECON, RS, 3>(nc, ring, params, offsets, nsolves, nwork, grid, s)
+                   : launch_batch_march_rs_nv<double, RECON, RS, 4>(nc, ring, params, offsets, nsolves, nwork, grid, s);
+  return nv == 3 ? launch_batch_march_rs_nv<float, RECON, RS, 3>(nc, ring, params, offsets, nsolves, nwork, grid, s)
+                 : launch_batch_march_rs_nv<float, RECON, RS, 4>(nc, ring, params, offsets, nsolves, nwork, grid, s);
 }
 
 template <typename Kernel>
@@ -699,6 +688,10 @@ int march_occupancy(Kernel kernel, size_t smem = 0) {
 // form, with the ring's shared memory where the ring is built.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 int march_single_occupancy() {
+  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
+    march_prefer_shared<stage_kernel_march_pk<NV, FORM, true>>();
+    return march_occupancy(stage_kernel_march_pk<NV, FORM, true>, march_smem<2>());
+  }
   constexpr bool ring = march_ring_on<R, RECON, NC>();
   if constexpr (ring) {
     march_prefer_shared<stage_kernel_march<R, RECON, RS, NV, NC, FORM, true>>();
@@ -708,32 +701,39 @@ int march_single_occupancy() {
 }
 
 template <typename R, int RECON, int RS, int NV, int NC>
-int march_blocks_per_sm_nv(bool batch, bool lean) {
-  if (batch) return march_occupancy(stage_kernel_batch_march<R, RECON, RS, NV, NC>);
+int march_blocks_per_sm_nv(int kind) {
+  if (kind == kMarchBatch || kind == kMarchBatchRing) {
+    if constexpr (march_ring_on<R, RECON, NC>()) {
+      if (kind == kMarchBatchRing) {
+        march_prefer_shared<stage_kernel_batch_march<R, RECON, RS, NV, NC, true>>();
+        return march_occupancy(stage_kernel_batch_march<R, RECON, RS, NV, NC, true>, march_smem<NC>());
+      }
+    }
+    return march_occupancy(stage_kernel_batch_march<R, RECON, RS, NV, NC>);
+  }
   if constexpr (sizeof(R) == 4 && NC > 1)
-    if (lean) return march_single_occupancy<R, RECON, RS, NV, NC, kMarchLeanBlend>();
+    if (kind == kMarchSingleLean) return march_single_occupancy<R, RECON, RS, NV, NC, kMarchLeanBlend>();
   return march_single_occupancy<R, RECON, RS, NV, NC, kMarchGeneric>();
 }
 
 template <typename R, int RECON, int RS, int NC>
-int march_blocks_per_sm_nc(int nv, bool batch, bool lean) {
-  return nv == 3 ? march_blocks_per_sm_nv<R, RECON, RS, 3, NC>(batch, lean)
-                 : march_blocks_per_sm_nv<R, RECON, RS, 4, NC>(batch, lean);
+int march_blocks_per_sm_nc(int nv, int kind) {
+  return nv == 3 ? march_blocks_per_sm_nv<R, RECON, RS, 3, NC>(kind) : march_blocks_per_sm_nv<R, RECON, RS, 4, NC>(kind);
 }
 
 template <typename R, int RECON, int RS>
-int march_blocks_per_sm_rs(int nv, int nc, bool batch, bool lean) {
+int march_blocks_per_sm_rs(int nv, int nc, int kind) {
   if constexpr (sizeof(R) == 4) {
-    if (nc == 1) return march_blocks_per_sm_nc<R, RECON, RS, 1>(nv, batch, lean);
-    if (nc == 3) return march_blocks_per_sm_nc<R, RECON, RS, 3>(nv, batch, lean);
+    if (nc == 1) return march_blocks_per_sm_nc<R, RECON, RS, 1>(nv, kind);
+    if (nc == 3) return march_blocks_per_sm_nc<R, RECON, RS, 3>(nv, kind);
   }
-  return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, batch, lean) : 0;
+  return nc == 2 ? march_blocks_per_sm_nc<R, RECON, RS, 2>(nv, kind) : 0;
 }
 
 template <int RECON, int RS>
-int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, bool batch, bool lean) {
-  return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, batch, lean)
-                         : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, batch, lean);
+int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, int kind) {
+  return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, kind)
+                         : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, kind);
 }
 
 }  // namespace jx

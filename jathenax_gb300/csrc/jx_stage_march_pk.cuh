@@ -1,0 +1,390 @@
+// Float32 marching stage for PPM4 + Roe (the inviscid "lean" forms, 3 or 4
+// variables, two columns per lane) with the lane's two columns held as
+// float32 pairs.
+//
+// The marching kernel is bound by instruction issue. Its lane holds columns
+// c0 and c0 + 1 of a 64-column strip and applies the same per-column
+// arithmetic to both; here every value of the walk is a float2 (column c0's,
+// column c0 + 1's) and every add, multiply and FMA of both sweeps is one
+// packed Blackwell instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn) for the
+// two columns. Comparisons, selects, min/max, the SFU reciprocal and root,
+// primitive recovery and the RK combine stay per column. The y sweep pairs
+// directly (each column's window, face value, edges and flux); the x sweep
+// pairs the two faces and two Riemann problems of the lane, whose operands
+// are built from the lane's pair and its neighbours' by register moves.
+//
+// Each packed operation rounds each half exactly as the corresponding
+// explicitly rounded float32 operation of jx_device.cuh (a - b is formed as
+// fma(b, -1, a), which rounds once, as a - b does), so the results are the
+// same bits as every other float32 stage kernel's (tested).
+#pragma once
+#include "jx_device.cuh"
+#include "jx_internal.h"
+#include "jx_ring.cuh"
+#include "jx_stage_fast.cuh"
+
+namespace jx {
+namespace pk {
+
+using F2 = float2;
+
+__device__ __forceinline__ F2 splat(float a) { return make_float2(a, a); }
+__device__ __forceinline__ F2 add(F2 a, F2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ F2 mul(F2 a, F2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ F2 fma(F2 a, F2 b, F2 c) { return __ffma2_rn(a, b, c); }
+// a - b rounded once: fma(b, -1, a) (the product is exact).
+__device__ __forceinline__ F2 sub(F2 a, F2 b) { return __ffma2_rn(b, splat(-1.f), a); }
+__device__ __forceinline__ F2 neg(F2 a) { return __fmul2_rn(a, splat(-1.f)); }
+__device__ __forceinline__ F2 abs2(F2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ F2 min2(F2 a, F2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+__device__ __forceinline__ F2 max2(F2 a, F2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
+__device__ __forceinline__ F2 rcp2(F2 a) { return make_float2(Num<float>::rcp(a.x), Num<float>::rcp(a.y)); }
+__device__ __forceinline__ F2 root2(F2 a) { return make_float2(Num<float>::root(a.x), Num<float>::root(a.y)); }
+__device__ __forceinline__ F2 sel(bool cx, bool cy, F2 a, F2 b) { return make_float2(cx ? a.x : b.x, cy ? a.y : b.y); }
+
+// The lane's two columns of one cell-sized quantity (component v: column
+// c0's in .x, column c0 + 1's in .y).
+struct PCell {
+  F2 v[4];
+};
+
+template <int NV>
+__device__ __forceinline__ PCell shfl_up(const PCell& c, int d) {
+  PCell o;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+    o.v[v] = v < NV ? make_float2(__shfl_up_sync(0xffffffffu, c.v[v].x, d), __shfl_up_sync(0xffffffffu, c.v[v].y, d))
+                    : splat(0.f);
+  return o;
+}
+
+template <int NV>
+__device__ __forceinline__ PCell shfl_down(const PCell& c, int d) {
+  PCell o;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+    o.v[v] = v < NV ? make_float2(__shfl_down_sync(0xffffffffu, c.v[v].x, d),
+                                  __shfl_down_sync(0xffffffffu, c.v[v].y, d))
+                    : splat(0.f);
+  return o;
+}
+
+// (a's column c0 + 1, b's column c0): the pair one column to the right of a.
+template <int NV>
+__device__ __forceinline__ PCell straddle(const PCell& a, const PCell& b) {
+  PCell o;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) o.v[v] = v < NV ? make_float2(a.v[v].y, b.v[v].x) : splat(0.f);
+  return o;
+}
+
+// (a's column c0 + 1, s): a's second half next to a per-column value.
+template <int NV>
+__device__ __forceinline__ PCell straddle(const PCell& a, const float (&s)[4]) {
+  PCell o;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) o.v[v] = v < NV ? make_float2(a.v[v].y, s[v]) : splat(0.f);
+  return o;
+}
+
+// (s, a's column c0).
+template <int NV>
+__device__ __forceinline__ PCell straddle(const float (&s)[4], const PCell& a) {
+  PCell o;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) o.v[v] = v < NV ? make_float2(s[v], a.v[v].x) : splat(0.f);
+  return o;
+}
+
+// ppm4_face (float32): the fourth-order interpolant bounded by the two
+// neighbours; min/max per half in the scalar operand order.
+__device__ __forceinline__ F2 ppm4_face2(F2 w0, F2 w1, F2 w2, F2 w3) {
+  const F2 e = mul(fma(splat(7.f), add(w2, w1), neg(add(w0, w3))), splat(float(1.0 / 12.0)));
+  return min2(max2(e, min2(w2, w1)), max2(w2, w1));
+}
+
+// ppm4_cell (float32 branch).
+__device__ __forceinline__ void ppm4_cell2(F2 c, F2 lo_face, F2 hi_face, F2& lo, F2& hi) {
+  const F2 dh = sub(hi_face, c), dl = sub(lo_face, c);
+  const F2 p = mul(dh, dl);
+  const F2 dh2 = mul(splat(2.f), abs2(dh)), dl2 = mul(splat(2.f), abs2(dl));
+  const bool flat_x = p.x >= 0.f, flat_y = p.y >= 0.f;
+  const bool slo_x = fabsf(dl.x) >= dh2.x, slo_y = fabsf(dl.y) >= dh2.y;
+  const bool shi_x = fabsf(dh.x) >= dl2.x, shi_y = fabsf(dh.y) >= dl2.y;
+  const F2 l2 = sel(slo_x, slo_y, fma(splat(-2.f), dh, c), lo_face);
+  const F2 h2 = sel(shi_x, shi_y, fma(splat(-2.f), dl, c), hi_face);
+  lo = sel(flat_x, flat_y, c, l2);
+  hi = sel(flat_x, flat_y, c, h2);
+}
+
+// flux_roe_f32 for both halves (fluxes.py:134-172).
+__device__ __forceinline__ void roe2(F2 dl, F2 dr, F2 ul, F2 ur, F2 tl, F2 tr, const Gas<float>& g, F2& f0, F2& f1,
+                                     F2& f2) {
+  const F2 cs = splat(g.cs), cs2 = splat(g.cs2), half = splat(0.5f), hic = splat(g.half_inv_cs);
+  const F2 ml = mul(dl, ul), mr = mul(dr, ur);
+  const F2 ql = mul(dl, tl), qr = mul(dr, tr);
+  const F2 s0 = add(ml, mr);
+  const F2 s1 = fma(ml, ul, fma(mr, ur, mul(cs2, add(dl, dr))));
+  const F2 s2 = fma(ml, tl, mul(mr, tr));
+  const F2 r = mul(root2(dl), root2(dr));
+  const F2 inv = rcp2(add(dl, r));
+  const F2 u = mul(fma(r, ur, ml), inv);
+  const F2 t = mul(fma(r, tr, ql), inv);
+  const F2 lm = sub(u, cs), lp = add(u, cs);
+  const F2 jd = sub(dr, dl), jm = sub(mr, ml), jq = sub(qr, ql);
+  const F2 hu = mul(u, hic);
+  const F2 jmc = mul(jm, hic);
+  const F2 am = fma(jd, add(half, hu), neg(jmc));
+  const F2 ap = fma(jd, sub(half, hu), jmc);
+  const F2 az = fma(jd, neg(t), jq);
+  const F2 wm = mul(abs2(lm), am), wz = mul(abs2(u), az), wp = mul(abs2(lp), ap);
+  const F2 wmp = add(wm, wp);
+  const F2 dstar = add(dl, am);
+  const F2 dstar2 = add(dstar, ap);
+  f0 = mul(half, sub(s0, wmp));
+  f1 = mul(half, sub(s1, fma(wm, lm, mul(wp, lp))));
+  f2 = mul(half, sub(s2, fma(wmp, t, wz)));
+  const bool bad_x = dstar.x < 0.f || dstar2.x < 0.f, bad_y = dstar.y < 0.f || dstar2.y < 0.f;
+  if (__builtin_expect(bad_x || bad_y, 0)) {  // positivity fix: rare
+    const F2 sp = mul(half, max2(add(abs2(ul), cs), add(abs2(ur), cs)));
+    const F2 nsp = neg(sp);
+    f0 = sel(bad_x, bad_y, fma(nsp, jd, mul(half, s0)), f0);
+    f1 = sel(bad_x, bad_y, fma(nsp, jm, mul(half, s1)), f1);
+    f2 = sel(bad_x, bad_y, fma(nsp, jq, mul(half, s2)), f2);
+  }
+}
+
+// face_flux_cells<roe> for both halves: Riemann flux in x/y component order
+// plus passive-scalar upwinding.
+template <int DIR, int NV>
+__device__ __forceinline__ PCell face_flux2(const PCell& L, const PCell& Rv, const Gas<float>& g) {
+  constexpr int nn = DIR == 0 ? 1 : 2, tt = DIR == 0 ? 2 : 1;
+  F2 f0, fn, ft;
+  roe2(L.v[0], Rv.v[0], L.v[nn], Rv.v[nn], L.v[tt], Rv.v[tt], g, f0, fn, ft);
+  PCell f;
+  f.v[0] = f0;
+  f.v[1] = DIR == 0 ? fn : ft;
+  f.v[2] = DIR == 0 ? ft : fn;
+  f.v[3] = splat(0.f);
+#pragma unroll
+  for (int v = 3; v < NV; ++v) f.v[v] = mul(f0, sel(f0.x >= 0.f, f0.y >= 0.f, L.v[v], Rv.v[v]));
+  return f;
+}
+
+template <int NV>
+__device__ __forceinline__ PCell faces2(const PCell& w0, const PCell& w1, const PCell& w2, const PCell& w3) {
+  PCell a;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) a.v[v] = v < NV ? ppm4_face2(w0.v[v], w1.v[v], w2.v[v], w3.v[v]) : splat(0.f);
+  return a;
+}
+
+template <int NV>
+__device__ __forceinline__ void edges2(const PCell& c, const PCell& lf, const PCell& hf, PCell& lo, PCell& hi) {
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    if (v < NV) ppm4_cell2(c.v[v], lf.v[v], hf.v[v], lo.v[v], hi.v[v]);
+    else lo.v[v] = hi.v[v] = splat(0.f);
+  }
+}
+
+// The lane's two cells (columns c0 and c0 + 1) recovered into a pair: the
+// density floor, then the primitives, per cell as recover_cell does.
+template <int NV>
+__device__ __forceinline__ PCell recover2(const Cell4<float>& a, const Cell4<float>& b, float dfloor) {
+  const float ra = Num<float>::lt(a.v[0], dfloor) ? dfloor : a.v[0];
+  const float rb = Num<float>::lt(b.v[0], dfloor) ? dfloor : b.v[0];
+  const float ia = Num<float>::rcp(ra), ib = Num<float>::rcp(rb);
+  PCell w;
+  w.v[0] = make_float2(ra, rb);
+#pragma unroll
+  for (int v = 1; v < 4; ++v) w.v[v] = v < NV ? make_float2(__fmul_rn(ia, a.v[v]), __fmul_rn(ib, b.v[v])) : splat(0.f);
+  return w;
+}
+
+// The lane's columns: the primitives of rows j-3 .. j (PPM4's edges need only
+// the cell itself, so the lean walk keeps 4 rows), the face value below row
+// j-1, the upper edge of row j-3 and the y flux below row j-3.
+struct ColumnPair {
+  PCell W3, W2, W1, W0, Ay2, hy3, Fy3;
+};
+
+// One tile of kMarchTileX (58) columns by p.ty rows, one warp, two columns
+// per lane (lane l: columns c0 = x0 - 3 + 2 l and c0 + 1), as march_tile in
+// jx_stage_march.cuh walks it, with the same row ring when RING.
+template <int NV, bool BLEND, bool RING>
+__device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, int ntiles, float4* ring) {
+  using N = Num<float>;
+  const StageConsts<float>& k = stage_consts<float>(p);
+  const int lane = threadIdx.x & 31;
+  const int TY = p.ty;
+  const int bx = tile % p.tiles_x, by = tile / p.tiles_x;
+  const int x0 = bx * kMarchTileX;
+  const int y0 = by * TY;
+  const int c0 = x0 - 3 + 2 * lane;
+  const int xlast = min(x0 + kMarchTileX, p.nx) - 1;
+  int gx[2], cx[2];
+  bool out[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    gx[h] = wrap_fast(c0 + h, p.nx);
+    const int local = 2 * lane + h;
+    out[h] = local >= 3 && local <= 60 && c0 + h < p.nx;
+    cx[h] = min(max(c0 + h, x0), xlast);
+  }
+  const float* __restrict__ U = static_cast<const float*>(p.U);
+  const float* __restrict__ V = static_cast<const float*>(p.V);
+  float* Uo = static_cast<float*>(p.Uout);
+  float* Vo = static_cast<float*>(p.Vout);
+  Gas<float> gas;
+  gas.cs = k.cs;
+  gas.cs2 = k.cs2;
+  gas.inv_cs = k.inv_cs;
+  gas.half_inv_cs = k.half_inv_cs;
+  gas.quarter_inv_cs = 0.5f * k.half_inv_cs;
+  const float sdt = static_cast<float>(p.beta * p.clock->dt);
+  const float ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
+
+  ColumnPair c;
+  c.W3 = c.W2 = c.W1 = c.W0 = c.Ay2 = c.hy3 = c.Fy3 = PCell{};
+  float vmax0 = 0.f, vmax1 = 0.f;
+  const int iters = TY + 6;
+  Cell4<float> next[2];
+  auto ringU = [&](int t, int h) { return ring + ((t & (kRingU - 1)) * 2 + h) * 32 + lane; };
+  auto ringV = [&](int t, int h) { return ring + (kRingU * 2 + (t & (kRingV - 1)) * 2 + h) * 32 + lane; };
+  if constexpr (RING) {
+    for (int t = 0; t < kRingAhead; ++t) {
+      const size_t row = (size_t)wrap_fast(y0 - 3 + t, p.ny) * p.nx;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) ring_copy<NV>(ringU(t, h), U + (row + gx[h]) * NV);
+      cp_async_commit();
+    }
+  } else {
+    const size_t row = (size_t)wrap_fast(y0 - 3, p.ny) * p.nx;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) next[h] = load_cell<float, NV>(U + (row + gx[h]) * NV);
+  }
+  auto walk_row = [&](const int it, auto steady_tag) {
+    constexpr bool kSteady = decltype(steady_tag)::value;
+    const int j = y0 - 3 + it;
+    if constexpr (RING) {
+      // As in march_tile: this row's U and the V the combine reads (row
+      // it - 3) came in group it of kRingAhead + it committed ones.
+      cp_async_wait<kRingAhead - 1>();
+#pragma unroll
+      for (int h = 0; h < 2; ++h) next[h] = ring_read<NV>(ringU(it, h));
+    }
+    c.W3 = c.W2;
+    c.W2 = c.W1;
+    c.W1 = c.W0;
+    c.W0 = recover2<NV>(next[0], next[1], k.dfloor);
+    if constexpr (RING) {
+      if (it + kRingAhead < iters) {
+        const size_t row = (size_t)wrap_fast(j + kRingAhead, p.ny) * p.nx;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) ring_copy<NV>(ringU(it + kRingAhead, h), U + (row + gx[h]) * NV);
+      }
+      if (it >= 3 && j < p.ny && it < TY + 3) {
+        const size_t row = (size_t)j * p.nx;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) ring_copy<NV>(ringV(it, h), V + (row + (size_t)cx[h]) * NV);
+      }
+      cp_async_commit();
+    } else {
+      const size_t row = (size_t)wrap_fast(j + 1, p.ny) * p.nx;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) next[h] = load_cell<float, NV>(U + (row + gx[h]) * NV);
+    }
+    // ---- y sweep of both columns -------------------------------------------
+    PCell Ay1 = c.Ay2;
+    if (kSteady || it >= 3) Ay1 = faces2<NV>(c.W3, c.W2, c.W1, c.W0);
+    PCell lo = c.hy3, hi = c.hy3;
+    if (kSteady || it >= 4) edges2<NV>(c.W2, c.Ay2, Ay1, lo, hi);
+    PCell Fy2 = c.Fy3;
+    if (kSteady || it >= 5) Fy2 = face_flux2<1, NV>(c.hy3, lo, gas);
+    if (kSteady) {
+      // ---- x sweep of row r = j-3 across the lanes -------------------------
+      const PCell& own = c.W3;                           // columns (c0, c0+1)
+      const PCell L = shfl_up<NV>(own, 1);               // (c0-2, c0-1)
+      const PCell R = shfl_down<NV>(own, 1);             // (c0+2, c0+3)
+      const PCell A01 = faces2<NV>(L, straddle<NV>(L, own), own, straddle<NV>(own, R));  // faces c0, c0+1
+      float A2[4], hiL[4], F2s[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) A2[v] = v < NV ? __shfl_down_sync(0xffffffffu, A01.v[v].x, 1) : 0.f;  // face c0+2
+      PCell lx, hx;
+      edges2<NV>(own, A01, straddle<NV>(A01, A2), lx, hx);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) hiL[v] = v < NV ? __shfl_up_sync(0xffffffffu, hx.v[v].y, 1) : 0.f;  // column c0-1
+      const PCell F01 = face_flux2<0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
+#pragma unroll
+      for (int v = 0; v < 4; ++v) F2s[v] = v < NV ? __shfl_down_sync(0xffffffffu, F01.v[v].x, 1) : 0.f;  // face c0+2
+      // The flux differences of both cells, each rounded on its own.
+      const PCell F12 = straddle<NV>(F01, F2s);
+      PCell dfx, dfy;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        dfx.v[v] = sub(F12.v[v], F01.v[v]);
+        dfy.v[v] = sub(Fy2.v[v], c.Fy3.v[v]);
+      }
+      const int r = j - 3;
+      if (r < p.ny) {
+        const size_t row = (size_t)r * p.nx;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const size_t cell = row + (size_t)cx[h];
+          Cell4<float> u, vs;
+          if constexpr (RING) {
+            u = ring_read<NV>(ringU(it - 3, h));
+            vs = ring_read<NV>(ringV(it - 3, h));
+          } else {
+            u = load_cell<float, NV>(U + cell * NV);
+            vs = load_cell<float, NV>(V + cell * NV);
+          }
+          u.v[0] = h == 0 ? own.v[0].x : own.v[0].y;  // the floored density
+          if (p.floor_v) vs.v[0] = N::lt(vs.v[0], k.dfloor) ? k.dfloor : vs.v[0];
+          Cell4<float> un;
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            if (p.has_delta) vs.v[v] = delta_update(vs.v[v], k.delta, u.v[v]);
+            un.v[v] = rk_combine<float>(BLEND, k.g0, k.g1, u.v[v], vs.v[v], h == 0 ? dfx.v[v].x : dfx.v[v].y,
+                                        h == 0 ? dfy.v[v].x : dfy.v[v].y, ncx, ncy);
+          }
+          un.v[3] = NV == 4 ? un.v[3] : 0.f;
+          if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
+          if (out[h]) {
+            if (p.has_delta && Vo) store_cell<float, NV>(Vo + cell * NV, vs);
+            store_cell<float, NV>(Uo + cell * NV, un);
+          }
+          if (p.want_cfl) {
+            const float inv = N::rcp(un.v[0]);
+            const float s0 = signal_speed(inv, un.v[1], k.cs), s1 = signal_speed(inv, un.v[2], k.cs);
+            if (out[h]) {
+              vmax0 = N::nanmax_pos(vmax0, s0);
+              vmax1 = N::nanmax_pos(vmax1, s1);
+            }
+          }
+        }
+      }
+    }
+    c.Ay2 = Ay1;
+    c.hy3 = hi;
+    c.Fy3 = Fy2;
+  };
+  for (int it = 0; it < 6; ++it) walk_row(it, Flag<false>{});
+#pragma unroll 1
+  for (int it = 6; it < iters; ++it) walk_row(it, Flag<true>{});
+  if constexpr (RING) cp_async_wait_all();
+  if (p.want_cfl) {
+    const double m0 = warp_nan_max(static_cast<double>(vmax0));
+    const double m1 = warp_nan_max(static_cast<double>(vmax1));
+    if (lane == 0) {
+      p.partials[(size_t)tile * kCflSlots + 0] = m0;
+      p.partials[(size_t)tile * kCflSlots + 1] = m1;
+      p.partials[(size_t)tile * kCflSlots + 2] = 0.0;
+      if (tile == 0) p.header->n_cfl = ntiles;
+    }
+  }
+}
+
+}  // namespace pk
+}  // namespace jx

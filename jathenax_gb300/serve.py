@@ -180,17 +180,21 @@ def _device_state(problem, n):
     return U
 
 
-def warmup_requests(dtypes=("float32", "float64")):
-    """One tiny request per problem, reconstruction, Riemann solver and precision:
-    running them once loads every kernel a stream can use (CUDA loads kernels
-    lazily, at their first launch), so a server's first requests do not pay for it."""
+def warmup_requests(dtypes=("float32", "float64"), sides=(16,)):
+    """One short request per problem, reconstruction, Riemann solver,
+    precision and side: running them once loads every kernel a stream can use
+    (CUDA loads kernels lazily, at their first launch), so a server's first
+    requests do not pay for it. With tuned tiles the size classes run
+    different kernels, so a server warms one side per class."""
     out = []
-    for dtype in dtypes:
-        for problem in PROBLEMS:
-            for recon in RECONS:
-                for rsolver in SOLVERS:
-                    out.append(Request(rid=-1 - len(out), arrival=0.0, problem=problem, side=16, reconstruct=recon,
-                                       rsolver=rsolver, tlim=0.004, dtype=dtype, seed=1))
+    for side in sides:
+        for dtype in dtypes:
+            for problem in PROBLEMS:
+                for recon in RECONS:
+                    for rsolver in SOLVERS:
+                        out.append(Request(rid=-1 - len(out), arrival=0.0, problem=problem, side=side,
+                                           reconstruct=recon, rsolver=rsolver, tlim=0.004 * 16 / side, dtype=dtype,
+                                           seed=1))
     return out
 
 
@@ -294,9 +298,11 @@ class Server:
                     for recon in RECONS:
                         self.tile_for(Request(rid=-1, arrival=0.0, problem="kh", side=min(top, side),
                                               reconstruct=recon, rsolver="roe", tlim=0.0, dtype=dtype, seed=1))
+        # One side per size class (its smallest) where the classes' tiles differ.
+        sides = (16,) if self.tile != "auto" else (16,) + tuple(top + 1 for top, _, _ in SIZE_CLASSES[:-1])
         forced, self.dtype = self.dtype, None  # each warm-up request in its own precision
         try:
-            self.run(warmup_requests(dtypes))
+            self.run(warmup_requests(dtypes, sides))
         finally:
             self.dtype = forced
 

@@ -82,7 +82,9 @@ def test_batch_mixes_tiles_and_kernels_bitwise():
     tiles = [(32, 16), (32, 8), (58, 8), (58, 32), (0, 0), (32, 32), (58, 64)]
     solves = [make_solve(*spec, tile_y=ty, tile_x=tx) for spec, (tx, ty) in zip(SPECS, tiles)]
     batch = Batch(solves)
-    assert batch.groups == 5  # the float32 ppm4/roe class runs both kernels
+    # The float32 ppm4/roe class runs both kernels, its 3-variable marching
+    # solves in two groups (8 rows: register path; 32 rows: the row ring).
+    assert batch.groups == 6
     batch.run(steps_per_sync=4)
     for spec, s, (tx, ty) in zip(SPECS, solves, tiles):
         U_alone, _, _ = run_alone(spec, ty, tx)
@@ -122,12 +124,14 @@ def test_batched_forcing_matches_solo_bitwise():
 
 def test_float32_batch_mixing_methods_and_columns_per_lane_is_bitwise():
     """Float32 solves of every reconstruction family in one batch, on marching
-    tiles of 1, 2 and 3 columns per lane and on the shared-memory tile: each
-    is bitwise its own solo run (and the solo runs agree across tiles)."""
+    tiles of 1, 2 and 3 columns per lane (short ones on the register path,
+    tall ones through the row ring where it is built) and on the
+    shared-memory tile: each is bitwise its own solo run (and the solo runs
+    agree across tiles)."""
     from jathenax_gb300.batch import Batch, ClockBank
     specs = [("kh", 40, "float32", "dc", "llf", "rk2", 0.03), ("kh", 52, "float32", "wenoz", "hlle", "rk3", 0.02),
              ("smooth", 44, "float32", "ppmx", "roe", "rk4", 0.02), ("turb", 36, "float32", "plm", "hlle", "rk3", 0.03)]
-    tiles = [(26, 8), (58, 12), (90, 8), (32, 16)]
+    tiles = [(26, 8), (58, 12), (90, 8), (32, 16), (26, 24), (58, 32), (90, 28)]
     bank = ClockBank(len(specs) * len(tiles))
     solves, expect = [], []
     for i, spec in enumerate(specs):

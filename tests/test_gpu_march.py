@@ -130,7 +130,8 @@ def test_columns_per_lane_do_not_change_results(rec, rs):
     import torch
     U0 = noisy_state(187, 70, nvar=4, seed=RECONS.index(rec) * 3 + SOLVERS.index(rs) + 40)
     base = stepped(U0, torch.float32, (58, 16), recon=rec, rsolver=rs, steps=2)
-    for tile in ((26, 16), (90, 12)):
+    # 24 rows and more: the cp.async row ring where it is built.
+    for tile in ((26, 16), (90, 12), (26, 24), (58, 40), (90, 28)):
         assert_bitwise(stepped(U0, torch.float32, tile, recon=rec, rsolver=rs, steps=2), base, f"{rec}/{rs} {tile}")
 
 
@@ -143,7 +144,7 @@ def test_columns_per_lane_viscous_drag_and_stress(integrator):
     kw = dict(viscosity=2e-3, smagorinsky_cs=0.2, drag_rate=0.3)
     tau = 1e-3 * np.random.default_rng(5).standard_normal((45, 131, 3))
     base = stepped(U0, torch.float32, (58, 12), integrator=integrator, rsolver="hlle", tau=tau, **kw)
-    for tile in ((26, 8), (90, 20)):
+    for tile in ((26, 8), (90, 20), (26, 30), (58, 24), (90, 45)):
         got = stepped(U0, torch.float32, tile, integrator=integrator, rsolver="hlle", tau=tau, **kw)
         assert_bitwise(got, base, f"{integrator} {tile}")
 
@@ -155,7 +156,7 @@ def test_columns_per_lane_on_tiny_and_ragged_grids(shape):
     U0 = noisy_state(nx, ny, nvar=4, seed=ny * nx)
     for rec in ("ppm4", "wenoz"):
         base = stepped(U0, torch.float32, (58, 8), recon=rec)
-        for tile in ((26, 8), (90, 8)):
+        for tile in ((26, 8), (90, 8), (26, 24), (58, 32)):
             assert_bitwise(stepped(U0, torch.float32, tile, recon=rec), base, f"{shape} {rec} {tile}")
 
 
