@@ -514,23 +514,23 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, 
 
 template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
 
-// PPM4 + Roe with 4 variables in a lean form with two columns per lane runs
-// the packed-pair walk of jx_stage_march_pk.cuh (float32): 0.2812 -> 0.2642
-// ms per 4096² stage (58 x 121), 0.0269 -> 0.0249 ms at 1024²; with 3
-// variables it measured 1 % slower (0.2379 -> 0.2404 ms), so it keeps the
+// PPM4 with 4 variables in a lean form with two columns per lane runs the
+// packed-pair walk of jx_stage_march_pk.cuh (float32): with Roe 0.2812 ->
+// 0.2642 ms per 4096² stage (58 x 121), 0.0269 -> 0.0249 ms at 1024²; with
+// 3 variables it measured 1 % slower (0.2379 -> 0.2404 ms), so it keeps the
 // per-column walk.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
-  return sizeof(R) == 4 && RECON == JX_PPM4 && RS == JX_ROE && NV == 4 && NC == 2 && FORM != kMarchGeneric;
+  return sizeof(R) == 4 && RECON == JX_PPM4 && NV == 4 && NC == 2 && FORM != kMarchGeneric;
 }
 
 static_assert(kMarchWarps == 1, "the packed-pair kernel takes one tile per single-warp block");
-template <int NV, int FORM, bool RING>
+template <int RS, int NV, int FORM, bool RING>
 __global__ void __launch_bounds__(32, 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
   if (p.clock->done) return;
   const int tile = blockIdx.x;
   if (tile >= ntiles) return;
   extern __shared__ float4 march_ring[];
-  pk::march_tile_pk<NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
+  pk::march_tile_pk<RS, NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
 }
 
 // Let a ring kernel have the largest shared-memory carve-out (once per kernel).
@@ -581,10 +581,10 @@ template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
     if (p.ty >= kRingMinRows) {
-      march_prefer_shared<stage_kernel_march_pk<NV, FORM, true>>();
-      stage_kernel_march_pk<NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
+      march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
+      stage_kernel_march_pk<RS, NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
     } else {
-      stage_kernel_march_pk<NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
+      stage_kernel_march_pk<RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
     }
     return cudaGetLastError();
   }
@@ -689,8 +689,8 @@ int march_occupancy(Kernel kernel, size_t smem = 0) {
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 int march_single_occupancy() {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
-    march_prefer_shared<stage_kernel_march_pk<NV, FORM, true>>();
-    return march_occupancy(stage_kernel_march_pk<NV, FORM, true>, march_smem<2>());
+    march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
+    return march_occupancy(stage_kernel_march_pk<RS, NV, FORM, true>, march_smem<2>());
   }
   constexpr bool ring = march_ring_on<R, RECON, NC>();
   if constexpr (ring) {

@@ -1,6 +1,6 @@
-// Float32 marching stage for PPM4 + Roe (the inviscid "lean" forms, 3 or 4
-// variables, two columns per lane) with the lane's two columns held as
-// float32 pairs.
+// Float32 marching stage for PPM4 with any Riemann solver (the inviscid
+// "lean" forms, 3 or 4 variables, two columns per lane) with the lane's two
+// columns held as float32 pairs.
 //
 // The marching kernel is bound by instruction issue. Its lane holds columns
 // c0 and c0 + 1 of a 64-column strip and applies the same per-column
@@ -154,13 +154,51 @@ __device__ __forceinline__ void roe2(F2 dl, F2 dr, F2 ul, F2 ur, F2 tl, F2 tr, c
   }
 }
 
-// face_flux_cells<roe> for both halves: Riemann flux in x/y component order
-// plus passive-scalar upwinding.
-template <int DIR, int NV>
+// flux_llf (float32 branch) for both halves (fluxes.py:175-183).
+__device__ __forceinline__ void llf2(F2 dl, F2 dr, F2 ul, F2 ur, F2 tl, F2 tr, const Gas<float>& g, F2& f0, F2& f1,
+                                     F2& f2) {
+  const F2 cs = splat(g.cs), half = splat(0.5f);
+  const F2 ml = mul(dl, ul), mr = mul(dr, ur);
+  const F2 ql = mul(dl, tl), qr = mul(dr, tr);
+  const F2 s0 = add(ml, mr);
+  const F2 s1 = fma(ml, ul, fma(mr, ur, mul(splat(g.cs2), add(dl, dr))));
+  const F2 s2 = fma(ml, tl, mul(mr, tr));
+  const F2 nsp = neg(max2(add(abs2(ul), cs), add(abs2(ur), cs)));
+  f0 = mul(half, fma(nsp, sub(dr, dl), s0));
+  f1 = mul(half, fma(nsp, sub(mr, ml), s1));
+  f2 = mul(half, fma(nsp, sub(qr, ql), s2));
+}
+
+// flux_hlle (float32 branch) for both halves (fluxes.py:186-201).
+__device__ __forceinline__ void hlle2(F2 dl, F2 dr, F2 ul, F2 ur, F2 tl, F2 tr, const Gas<float>& g, F2& f0, F2& f1,
+                                      F2& f2) {
+  const F2 cs = splat(g.cs), cs2 = splat(g.cs2), half = splat(0.5f);
+  const F2 r = mul(root2(dl), root2(dr));
+  const F2 u = mul(fma(r, ur, mul(dl, ul)), rcp2(add(dl, r)));
+  const F2 alo = min2(sub(u, cs), sub(ul, cs));
+  const F2 ahi = max2(add(u, cs), add(ur, cs));
+  const F2 bm = sel(alo.x < 0.f, alo.y < 0.f, alo, splat(-1e-20f));
+  const F2 bp = sel(ahi.x > 0.f, ahi.y > 0.f, ahi, splat(1e-20f));
+  const F2 vl = sub(ul, bm), vr = sub(ur, bp);
+  const F2 ml = mul(dl, ul), mr = mul(dr, ur);
+  const F2 fl0 = mul(dl, vl), fl1 = fma(ml, vl, mul(cs2, dl)), fl2 = mul(mul(dl, tl), vl);
+  const F2 fr0 = mul(dr, vr), fr1 = fma(mr, vr, mul(cs2, dr)), fr2 = mul(mul(dr, tr), vr);
+  const F2 num = mul(half, add(bp, bm)), den = sub(bp, bm);
+  const F2 w = make_float2(Num<float>::quick_div(num.x, den.x), Num<float>::quick_div(num.y, den.y));
+  f0 = fma(w, sub(fl0, fr0), mul(half, add(fl0, fr0)));
+  f1 = fma(w, sub(fl1, fr1), mul(half, add(fl1, fr1)));
+  f2 = fma(w, sub(fl2, fr2), mul(half, add(fl2, fr2)));
+}
+
+// face_flux_cells for both halves: Riemann flux in x/y component order plus
+// passive-scalar upwinding.
+template <int RS, int DIR, int NV>
 __device__ __forceinline__ PCell face_flux2(const PCell& L, const PCell& Rv, const Gas<float>& g) {
   constexpr int nn = DIR == 0 ? 1 : 2, tt = DIR == 0 ? 2 : 1;
   F2 f0, fn, ft;
-  roe2(L.v[0], Rv.v[0], L.v[nn], Rv.v[nn], L.v[tt], Rv.v[tt], g, f0, fn, ft);
+  if constexpr (RS == JX_LLF) llf2(L.v[0], Rv.v[0], L.v[nn], Rv.v[nn], L.v[tt], Rv.v[tt], g, f0, fn, ft);
+  else if constexpr (RS == JX_HLLE) hlle2(L.v[0], Rv.v[0], L.v[nn], Rv.v[nn], L.v[tt], Rv.v[tt], g, f0, fn, ft);
+  else roe2(L.v[0], Rv.v[0], L.v[nn], Rv.v[nn], L.v[tt], Rv.v[tt], g, f0, fn, ft);
   PCell f;
   f.v[0] = f0;
   f.v[1] = DIR == 0 ? fn : ft;
@@ -212,7 +250,7 @@ struct ColumnPair {
 // One tile of kMarchTileX (58) columns by p.ty rows, one warp, two columns
 // per lane (lane l: columns c0 = x0 - 3 + 2 l and c0 + 1), as march_tile in
 // jx_stage_march.cuh walks it, with the same row ring when RING.
-template <int NV, bool BLEND, bool RING>
+template <int RS, int NV, bool BLEND, bool RING>
 __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, int ntiles, float4* ring) {
   using N = Num<float>;
   const StageConsts<float>& k = stage_consts<float>(p);
@@ -301,7 +339,7 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
     PCell lo = c.hy3, hi = c.hy3;
     if (kSteady || it >= 4) edges2<NV>(c.W2, c.Ay2, Ay1, lo, hi);
     PCell Fy2 = c.Fy3;
-    if (kSteady || it >= 5) Fy2 = face_flux2<1, NV>(c.hy3, lo, gas);
+    if (kSteady || it >= 5) Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
     if (kSteady) {
       // ---- x sweep of row r = j-3 across the lanes -------------------------
       const PCell& own = c.W3;                           // columns (c0, c0+1)
@@ -315,7 +353,7 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
       edges2<NV>(own, A01, straddle<NV>(A01, A2), lx, hx);
 #pragma unroll
       for (int v = 0; v < 4; ++v) hiL[v] = v < NV ? __shfl_up_sync(0xffffffffu, hx.v[v].y, 1) : 0.f;  // column c0-1
-      const PCell F01 = face_flux2<0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
+      const PCell F01 = face_flux2<RS, 0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
 #pragma unroll
       for (int v = 0; v < 4; ++v) F2s[v] = v < NV ? __shfl_down_sync(0xffffffffu, F01.v[v].x, 1) : 0.f;  // face c0+2
       // The flux differences of both cells, each rounded on its own.
