@@ -522,6 +522,12 @@ template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_byte
 template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
   return sizeof(R) == 4 && RECON == JX_PPM4 && NV == 4 && NC == 2 && FORM != kMarchGeneric;
 }
+// On tall tiles the packed walk with the row ring runs for Roe and HLLE
+// (4096²: 0.2818 -> 0.2647 and 0.2886 -> 0.2717 ms); LLF's, which needs one
+// more register than fits 16 warps, was slower than the per-column ring walk
+// (0.2437 -> 0.2618 ms) and is not used (on short tiles, without the ring,
+// it gains: 0.0221 -> 0.0208 ms at 1024²).
+template <int RS> constexpr bool march_packed_ring() { return RS != JX_LLF; }
 
 static_assert(kMarchWarps == 1, "the packed-pair kernel takes one tile per single-warp block");
 template <int RS, int NV, int FORM, bool RING>
@@ -580,13 +586,15 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
-    if (p.ty >= kRingMinRows) {
+    if (p.ty < kRingMinRows) {
+      stage_kernel_march_pk<RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
+      return cudaGetLastError();
+    }
+    if constexpr (march_packed_ring<RS>()) {
       march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
       stage_kernel_march_pk<RS, NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
-    } else {
-      stage_kernel_march_pk<RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
+      return cudaGetLastError();
     }
-    return cudaGetLastError();
   }
   if constexpr (march_ring_on<R, RECON, NC>()) {
     if (p.ty >= kRingMinRows) {
@@ -688,7 +696,7 @@ int march_occupancy(Kernel kernel, size_t smem = 0) {
 // form, with the ring's shared memory where the ring is built.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 int march_single_occupancy() {
-  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
+  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>() && march_packed_ring<RS>()) {
     march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
     return march_occupancy(stage_kernel_march_pk<RS, NV, FORM, true>, march_smem<2>());
   }
