@@ -514,29 +514,35 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, 
 
 template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
 
-// PPM4 with 4 variables in a lean form with two columns per lane runs the
-// packed-pair walk of jx_stage_march_pk.cuh (float32): with Roe 0.2812 ->
-// 0.2642 ms per 4096² stage (58 x 121), 0.0269 -> 0.0249 ms at 1024²; with
-// 3 variables it measured 1 % slower (0.2379 -> 0.2404 ms), so it keeps the
-// per-column walk.
+// PLM, PPM4 and WENO-Z with 4 variables in a lean form with two columns per
+// lane run the packed-pair walk of jx_stage_march_pk.cuh (float32) where it
+// measured faster than the per-column walk (GB300, RK3 stage 2):
+//   * PPM4/Roe 0.2812 -> 0.2642 ms at 4096² (58 x 121, with the row ring),
+//     0.0269 -> 0.0249 ms at 1024² (58 x 8); HLLE 0.2886 -> 0.2717 and
+//     0.0270 -> 0.0250 ms; LLF 0.0221 -> 0.0208 ms at 1024², but its ring
+//     kernel spills (0.2437 -> 0.2618 ms), so LLF's tall tiles keep the
+//     per-column ring walk;
+//   * PLM/HLLE 0.3466 -> 0.3259 ms at 4096², 0.0311 -> 0.0290 ms at 1024²;
+//   * WENO-Z/HLLE on 58 x 121 tiles 1.481 -> 1.344 ms, but on the 8-row
+//     tiles of a 1024² grid 0.123 -> 0.156 ms, so only tall tiles use it
+//     (WENO-Z defaults to one column per lane, which it does not cover);
+//   * DC: 0.176 -> 0.202 ms at 4096², 0.0144 ms either way at 1024²: not used.
+// With 3 variables PPM4 measured 1 % slower (0.2379 -> 0.2404 ms): not used.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
-  return sizeof(R) == 4 && RECON == JX_PPM4 && NV == 4 && NC == 2 && FORM != kMarchGeneric;
+  return sizeof(R) == 4 && (RECON == JX_PLM || RECON == JX_PPM4 || RECON == JX_WENOZ) && NV == 4 && NC == 2 &&
+         FORM != kMarchGeneric;
 }
-// On tall tiles the packed walk with the row ring runs for Roe and HLLE
-// (4096²: 0.2818 -> 0.2647 and 0.2886 -> 0.2717 ms); LLF's, which needs one
-// more register than fits 16 warps, was slower than the per-column ring walk
-// (0.2437 -> 0.2618 ms) and is not used (on short tiles, without the ring,
-// it gains: 0.0221 -> 0.0208 ms at 1024²).
-template <int RS> constexpr bool march_packed_ring() { return RS != JX_LLF; }
+template <int RECON> constexpr bool march_packed_short() { return RECON != JX_WENOZ; }
+template <int RECON, int RS> constexpr bool march_packed_ring() { return RECON != JX_PPM4 || RS != JX_LLF; }
 
 static_assert(kMarchWarps == 1, "the packed-pair kernel takes one tile per single-warp block");
-template <int RS, int NV, int FORM, bool RING>
-__global__ void __launch_bounds__(32, 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
+template <int RECON, int RS, int NV, int FORM, bool RING>
+__global__ void __launch_bounds__(32, RECON == JX_WENOZ ? 12 : 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
   if (p.clock->done) return;
   const int tile = blockIdx.x;
   if (tile >= ntiles) return;
   extern __shared__ float4 march_ring[];
-  pk::march_tile_pk<RS, NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
+  pk::march_tile_pk<RECON, RS, NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
 }
 
 // Let a ring kernel have the largest shared-memory carve-out (once per kernel).
@@ -587,12 +593,13 @@ template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
     if (p.ty < kRingMinRows) {
-      stage_kernel_march_pk<RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
-      return cudaGetLastError();
-    }
-    if constexpr (march_packed_ring<RS>()) {
-      march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
-      stage_kernel_march_pk<RS, NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
+      if constexpr (march_packed_short<RECON>()) {
+        stage_kernel_march_pk<RECON, RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
+        return cudaGetLastError();
+      }
+    } else if constexpr (march_packed_ring<RECON, RS>()) {
+      march_prefer_shared<stage_kernel_march_pk<RECON, RS, NV, FORM, true>>();
+      stage_kernel_march_pk<RECON, RS, NV, FORM, true><<<blocks, threads, march_smem<2>(), s>>>(p, ntiles);
       return cudaGetLastError();
     }
   }
@@ -696,9 +703,9 @@ int march_occupancy(Kernel kernel, size_t smem = 0) {
 // form, with the ring's shared memory where the ring is built.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 int march_single_occupancy() {
-  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>() && march_packed_ring<RS>()) {
-    march_prefer_shared<stage_kernel_march_pk<RS, NV, FORM, true>>();
-    return march_occupancy(stage_kernel_march_pk<RS, NV, FORM, true>, march_smem<2>());
+  if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>() && march_packed_ring<RECON, RS>()) {
+    march_prefer_shared<stage_kernel_march_pk<RECON, RS, NV, FORM, true>>();
+    return march_occupancy(stage_kernel_march_pk<RECON, RS, NV, FORM, true>, march_smem<2>());
   }
   constexpr bool ring = march_ring_on<R, RECON, NC>();
   if constexpr (ring) {

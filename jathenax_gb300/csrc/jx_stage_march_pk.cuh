@@ -1,6 +1,8 @@
-// Float32 marching stage for PPM4 with any Riemann solver (the inviscid
-// "lean" forms, 3 or 4 variables, two columns per lane) with the lane's two
-// columns held as float32 pairs.
+// Float32 marching stage (DC, PLM, PPM4 or WENO-Z edges, any Riemann solver,
+// the inviscid "lean" forms, 3 or 4 variables, two columns per lane) with the
+// lane's two columns held as float32 pairs. Which (reconstruction, solver,
+// variables, tile) combinations use it is decided by measurement; see
+// march_packed in jx_stage_march.cuh.
 //
 // The marching kernel is bound by instruction issue. Its lane holds columns
 // c0 and c0 + 1 of a 64-column strip and applies the same per-column
@@ -217,12 +219,76 @@ __device__ __forceinline__ PCell faces2(const PCell& w0, const PCell& w1, const 
   return a;
 }
 
-template <int NV>
-__device__ __forceinline__ void edges2(const PCell& c, const PCell& lf, const PCell& hf, PCell& lo, PCell& hi) {
+__device__ __forceinline__ F2 div2(F2 a, F2 b) { return make_float2(Num<float>::div(a.x, b.x), Num<float>::div(a.y, b.y)); }
+
+// plm_cell (float32) for both halves (fluxes.py:11-18, harmonic-mean slope).
+__device__ __forceinline__ void plm_cell2(F2 m1, F2 c, F2 p1, F2& lo, F2& hi) {
+  const F2 bw = sub(c, m1), fw = sub(p1, c);
+  const F2 p = mul(bw, fw), s = add(bw, fw);
+  const F2 hs = make_float2(p.x > 0.f ? Num<float>::quick_div(p.x, s.x) : 0.f,
+                            p.y > 0.f ? Num<float>::quick_div(p.y, s.y) : 0.f);
+  hi = add(c, hs);
+  lo = sub(c, hs);
+}
+
+// wenoz_combine (float32) for both halves (fluxes.py:87-93).
+__device__ __forceinline__ F2 wenoz_combine2(F2 s0, F2 s1, F2 s2, F2 s3, F2 s4, F2 w0, F2 w1, F2 w2) {
+  const F2 a0 = mul(splat(0.1f), w0), a1 = mul(splat(0.6f), w1), a2 = mul(splat(0.3f), w2);
+  const F2 f0 = fma(splat(11.f), s2, fma(splat(-7.f), s1, mul(splat(2.f), s0)));
+  const F2 f1 = fma(splat(2.f), s3, fma(splat(5.f), s2, neg(s1)));
+  const F2 f2 = sub(fma(splat(5.f), s3, mul(splat(2.f), s2)), s4);
+  const F2 num = fma(f2, a2, fma(f1, a1, mul(f0, a0)));
+  return div2(num, mul(splat(6.f), add(add(a0, a1), a2)));
+}
+
+// wenoz_cell_f32 for both halves (fluxes.py:96-117).
+__device__ __forceinline__ void wenoz_cell2(F2 m2, F2 m1, F2 c, F2 p1, F2 p2, F2& lo, F2& hi) {
+  const F2 k1312 = splat(float(13.0 / 12.0)), q = splat(0.25f);
+  const F2 eps = splat(1e-42f > Tiny<float>::value ? 1e-42f : Tiny<float>::value);
+  const F2 t0 = fma(splat(-2.f), m1, add(m2, c)), u0 = fma(splat(-4.f), m1, fma(splat(3.f), c, m2));
+  const F2 t1 = fma(splat(-2.f), c, add(m1, p1)), u1 = sub(m1, p1);
+  const F2 t2 = fma(splat(-2.f), p1, add(p2, c)), u2 = fma(splat(-4.f), p1, fma(splat(3.f), c, p2));
+  const F2 b0 = fma(k1312, mul(t0, t0), mul(q, mul(u0, u0)));
+  const F2 b1 = fma(k1312, mul(t1, t1), mul(q, mul(u1, u1)));
+  const F2 b2 = fma(k1312, mul(t2, t2), mul(q, mul(u2, u2)));
+  const F2 tau = abs2(sub(b0, b2));
+  const F2 d0 = add(b0, eps), d1 = add(b1, eps), d2 = add(b2, eps);
+  const F2 dmin = min2(d0, min2(d1, d2));
+  const F2 inv_sc = div2(splat(1.f), max2(tau, dmin));
+  F2 base = mul(dmin, inv_sc);
+  base = mul(base, base);
+  const F2 con = mul(tau, inv_sc);
+  const F2 r0 = mul(con, div2(dmin, d0)), r1 = mul(con, div2(dmin, d1)), r2 = mul(con, div2(dmin, d2));
+  const F2 w0 = fma(r0, r0, base), w1 = fma(r1, r1, base), w2 = fma(r2, r2, base);
+  hi = wenoz_combine2(m2, m1, c, p1, p2, w0, w1, w2);
+  lo = wenoz_combine2(p2, p1, c, m1, m2, w2, w1, w0);
+}
+
+// edges_cells for both halves: the low/high edges of the cells at the
+// centre of (m2, m1, c, p1, p2); lf/hf the face values (PPM4 only).
+template <int RECON, int NV>
+__device__ __forceinline__ void edges2(const PCell& m2, const PCell& m1, const PCell& c, const PCell& p1,
+                                       const PCell& p2, const PCell& lf, const PCell& hf, float dfloor, PCell& lo,
+                                       PCell& hi) {
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    if (v < NV) ppm4_cell2(c.v[v], lf.v[v], hf.v[v], lo.v[v], hi.v[v]);
-    else lo.v[v] = hi.v[v] = splat(0.f);
+    if (v < NV) {
+      if constexpr (RECON == JX_DC) {
+        lo.v[v] = hi.v[v] = c.v[v];
+      } else if constexpr (RECON == JX_PLM) {
+        plm_cell2(m1.v[v], c.v[v], p1.v[v], lo.v[v], hi.v[v]);
+      } else if constexpr (RECON == JX_PPM4) {
+        ppm4_cell2(c.v[v], lf.v[v], hf.v[v], lo.v[v], hi.v[v]);
+      } else {
+        wenoz_cell2(m2.v[v], m1.v[v], c.v[v], p1.v[v], p2.v[v], lo.v[v], hi.v[v]);
+      }
+    } else {
+      lo.v[v] = hi.v[v] = splat(0.f);
+    }
+  }
+  if constexpr (RECON == JX_WENOZ) {  // fluxes.py:128-130
+    lo.v[0] = max2(lo.v[0], splat(dfloor));
+    hi.v[0] = max2(hi.v[0], splat(dfloor));
   }
 }
 
@@ -240,17 +306,17 @@ __device__ __forceinline__ PCell recover2(const Cell4<float>& a, const Cell4<flo
   return w;
 }
 
-// The lane's columns: the primitives of rows j-3 .. j (PPM4's edges need only
-// the cell itself, so the lean walk keeps 4 rows), the face value below row
-// j-1, the upper edge of row j-3 and the y flux below row j-3.
+// The lane's columns: the primitives of rows j-4 .. j (only WENO-Z reads
+// row j-4), the face value below row j-1 (PPM4), the upper edge of row j-3
+// and the y flux below row j-3.
 struct ColumnPair {
-  PCell W3, W2, W1, W0, Ay2, hy3, Fy3;
+  PCell W4, W3, W2, W1, W0, Ay2, hy3, Fy3;
 };
 
 // One tile of kMarchTileX (58) columns by p.ty rows, one warp, two columns
 // per lane (lane l: columns c0 = x0 - 3 + 2 l and c0 + 1), as march_tile in
 // jx_stage_march.cuh walks it, with the same row ring when RING.
-template <int RS, int NV, bool BLEND, bool RING>
+template <int RECON, int RS, int NV, bool BLEND, bool RING>
 __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, int ntiles, float4* ring) {
   using N = Num<float>;
   const StageConsts<float>& k = stage_consts<float>(p);
@@ -284,7 +350,7 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
   const float ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
 
   ColumnPair c;
-  c.W3 = c.W2 = c.W1 = c.W0 = c.Ay2 = c.hy3 = c.Fy3 = PCell{};
+  c.W4 = c.W3 = c.W2 = c.W1 = c.W0 = c.Ay2 = c.hy3 = c.Fy3 = PCell{};
   float vmax0 = 0.f, vmax1 = 0.f;
   const int iters = TY + 6;
   Cell4<float> next[2];
@@ -312,6 +378,7 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
 #pragma unroll
       for (int h = 0; h < 2; ++h) next[h] = ring_read<NV>(ringU(it, h));
     }
+    c.W4 = c.W3;
     c.W3 = c.W2;
     c.W2 = c.W1;
     c.W1 = c.W0;
@@ -335,9 +402,10 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
     }
     // ---- y sweep of both columns -------------------------------------------
     PCell Ay1 = c.Ay2;
-    if (kSteady || it >= 3) Ay1 = faces2<NV>(c.W3, c.W2, c.W1, c.W0);
+    if constexpr (RECON == JX_PPM4)
+      if (kSteady || it >= 3) Ay1 = faces2<NV>(c.W3, c.W2, c.W1, c.W0);
     PCell lo = c.hy3, hi = c.hy3;
-    if (kSteady || it >= 4) edges2<NV>(c.W2, c.Ay2, Ay1, lo, hi);
+    if (kSteady || it >= 4) edges2<RECON, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1, k.dfloor, lo, hi);
     PCell Fy2 = c.Fy3;
     if (kSteady || it >= 5) Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
     if (kSteady) {
@@ -345,12 +413,19 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
       const PCell& own = c.W3;                           // columns (c0, c0+1)
       const PCell L = shfl_up<NV>(own, 1);               // (c0-2, c0-1)
       const PCell R = shfl_down<NV>(own, 1);             // (c0+2, c0+3)
-      const PCell A01 = faces2<NV>(L, straddle<NV>(L, own), own, straddle<NV>(own, R));  // faces c0, c0+1
-      float A2[4], hiL[4], F2s[4];
+      const PCell m1 = straddle<NV>(L, own);             // (c0-1, c0)
+      const PCell p1 = straddle<NV>(own, R);             // (c0+1, c0+2)
+      PCell lf = own, hf = own;
+      if constexpr (RECON == JX_PPM4) {
+        lf = faces2<NV>(L, m1, own, p1);  // faces c0, c0+1
+        float A2[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) A2[v] = v < NV ? __shfl_down_sync(0xffffffffu, A01.v[v].x, 1) : 0.f;  // face c0+2
+        for (int v = 0; v < 4; ++v) A2[v] = v < NV ? __shfl_down_sync(0xffffffffu, lf.v[v].x, 1) : 0.f;  // face c0+2
+        hf = straddle<NV>(lf, A2);
+      }
+      float hiL[4], F2s[4];
       PCell lx, hx;
-      edges2<NV>(own, A01, straddle<NV>(A01, A2), lx, hx);
+      edges2<RECON, NV>(L, m1, own, p1, R, lf, hf, k.dfloor, lx, hx);
 #pragma unroll
       for (int v = 0; v < 4; ++v) hiL[v] = v < NV ? __shfl_up_sync(0xffffffffu, hx.v[v].y, 1) : 0.f;  // column c0-1
       const PCell F01 = face_flux2<RS, 0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
