@@ -722,16 +722,20 @@ jx_status jx_probe_math(int32_t dtype, int64_t n, const void* a, const void* b, 
 namespace {
 
 constexpr uint32_t kPlanMagic = 0x4a584250;  // "JXBP"
-// 2 precisions x 5 reconstructions x 3 solvers x 13 kernel classes (shared
+// 2 precisions x 5 reconstructions x 3 solvers x 19 kernel classes (shared
 // memory; marching with 3 or 4 variables at 1, 2 or 3 columns per lane, with
-// or without the row ring)
-constexpr int kMaxGroups = 390;
+// or without the row ring; lean 4-variable two-column groups per integrator,
+// with or without the ring)
+constexpr int kMaxGroups = 570;
 
 struct BatchGroup {
   int dtype, recon, rsolver, first, count, tile_first, nwork, march;
   int nv;   // marching groups: the variable count of every solve (0 in shared-memory groups)
   int nc;   // marching groups: columns per lane (0 in shared-memory groups)
-  int ring;  // marching groups: the row-ring kernel runs (member tiles of kRingMinRows rows or more)
+  int ring;  // marching groups: tiles of kRingMinRows rows or more, where a ring kernel runs
+  int lean;  // marching groups of inviscid 4-variable float32 solves with one integrator
+  int integrator;  // lean groups: the members' integrator (-1 otherwise)
+  int form[4];     // lean groups: the MarchForm of each stage
   int bps;  // resident blocks per SM of the group's kernel (occupancy at plan time)
   size_t smem;
 };
@@ -818,24 +822,26 @@ cudaError_t launch_batch(int recon, int dtype, int rsolver, const StageParams* p
   }
 }
 
-int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc, int ring) {
+int batch_march_occupancy(int recon, int dtype, int rsolver, int nv, int nc, int ring, int lean) {
+  const int kind = lean ? (ring ? kMarchBatchPackedRing : kMarchBatchPacked) : (ring ? kMarchBatchRing : kMarchBatch);
   switch (recon) {
-    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
-    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
-    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
-    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
-    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, ring ? kMarchBatchRing : kMarchBatch);
+    case JX_DC: return march_blocks_per_sm_dc(dtype, rsolver, nv, nc, kind);
+    case JX_PLM: return march_blocks_per_sm_plm(dtype, rsolver, nv, nc, kind);
+    case JX_PPM4: return march_blocks_per_sm_ppm4(dtype, rsolver, nv, nc, kind);
+    case JX_PPMX: return march_blocks_per_sm_ppmx(dtype, rsolver, nv, nc, kind);
+    default: return march_blocks_per_sm_wenoz(dtype, rsolver, nv, nc, kind);
   }
 }
 
-cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, int nc, int ring, const StageParams* params,
-                               const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+cudaError_t launch_batch_march(int recon, int dtype, int rsolver, int nv, int nc, int ring, int form,
+                               const StageParams* params, const int* offsets, int nsolves, int nwork, dim3 grid,
+                               cudaStream_t s) {
   switch (recon) {
-    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    default: return launch_batch_march_wenoz(dtype, rsolver, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    case JX_DC: return launch_batch_march_dc(dtype, rsolver, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    case JX_PLM: return launch_batch_march_plm(dtype, rsolver, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPM4: return launch_batch_march_ppm4(dtype, rsolver, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    case JX_PPMX: return launch_batch_march_ppmx(dtype, rsolver, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    default: return launch_batch_march_wenoz(dtype, rsolver, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
   }
 }
 
@@ -942,11 +948,18 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
     const int march = tl[i].march ? 1 : 0;
     const int nv = march ? d.nvar : 0;
     const int nc = march ? tl[i].mnc : 0;
-    const int ring = march && march_ring_built(d.dtype == JX_F32, d.recon, nc) && tl[i].mty >= kRingMinRows;
+    // Lean groups (no viscosity, Smagorinsky or drag; 4 variables, two
+    // columns per lane, float32; one integrator, so every member's stage has
+    // the same form) may run the packed walk, with or without the ring.
+    const int lean = march && d.dtype == JX_F32 && d.nvar == 4 && nc == 2 && d.viscosity == 0.0 &&
+                     d.smagorinsky_cs == 0.0 && d.drag_rate == 0.0;
+    const int integrator = lean ? d.integrator : -1;
+    const int ring = march && tl[i].mty >= kRingMinRows && (lean || march_ring_built(d.dtype == JX_F32, d.recon, nc));
     int g = 0;
     while (g < n_groups && !(h->groups[g].dtype == d.dtype && h->groups[g].recon == d.recon &&
                              h->groups[g].rsolver == d.rsolver && h->groups[g].march == march &&
-                             h->groups[g].nv == nv && h->groups[g].nc == nc && h->groups[g].ring == ring))
+                             h->groups[g].nv == nv && h->groups[g].nc == nc && h->groups[g].ring == ring &&
+                             h->groups[g].lean == lean && h->groups[g].integrator == integrator))
       ++g;
     if (g == n_groups) {
       if (n_groups == kMaxGroups) return fail(JX_ERR_INVALID, "more than %d solver groups", kMaxGroups);
@@ -958,6 +971,9 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
       G.nv = nv;
       G.nc = nc;
       G.ring = ring;
+      G.lean = lean;
+      G.integrator = integrator;
+      for (int k = 0; k < 4; ++k) G.form[k] = kMarchGeneric;
       G.smem = 0;
     }
     if (!march && tl[i].fast_smem > h->groups[g].smem) h->groups[g].smem = tl[i].fast_smem;
@@ -1008,6 +1024,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
           P.nc = t.mnc;
           P.ty = t.mty;
           P.tiles_x = t.mtiles_x;
+          if (G.lean) G.form[stage - 1] = P.blend ? kMarchLeanBlend : kMarchLeanPlain;
         }
         in = out;
       }
@@ -1019,7 +1036,7 @@ jx_status jx_batch_plan(const jx_solve* solves, int32_t n, void* plan, size_t by
   h->n_groups = n_groups;
   for (int g = 0; g < n_groups; ++g) {
     BatchGroup& G = h->groups[g];
-    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring)
+    G.bps = G.march ? batch_march_occupancy(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring, G.lean)
                     : batch_occupancy(G.recon, G.dtype, G.rsolver, G.smem);
     if (G.bps < 1) {
       cudaGetLastError();  // no device to query: one block per SM
@@ -1122,7 +1139,8 @@ jx_status jx_batch_step(const void* plan, const void* plan_dev, int32_t blocks_p
       const int* offs = offsets_dev + G.tile_first;
       cudaStream_t gs = side ? side->s[g % kSideStreams] : s;
       const cudaError_t e =
-          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring, P, offs, G.count, G.nwork,
+          G.march ? launch_batch_march(G.recon, G.dtype, G.rsolver, G.nv, G.nc, G.ring,
+                                       G.lean ? G.form[stage - 1] : kMarchGeneric, P, offs, G.count, G.nwork,
                                        dim3((unsigned)blocks), gs)
                   : launch_batch(G.recon, G.dtype, G.rsolver, P, offs, G.count, G.nwork, dim3((unsigned)blocks),
                                  G.smem, gs);

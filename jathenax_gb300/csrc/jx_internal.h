@@ -132,7 +132,20 @@ __host__ __device__ constexpr bool march_ring_built(bool f32, int recon, int nc)
   return f32 && recon != JX_DC && (recon != JX_WENOZ || nc == 1);
 }
 // Which marching kernel an occupancy query is for.
-enum MarchKind { kMarchSingle = 0, kMarchSingleLean = 1, kMarchBatch = 2, kMarchBatchRing = 3 };
+enum MarchKind {
+  kMarchSingle = 0,
+  kMarchSingleLean = 1,
+  kMarchBatch = 2,
+  kMarchBatchRing = 3,
+  kMarchBatchPacked = 4,      // a lean 4-variable group: the packed walk where it is used
+  kMarchBatchPackedRing = 5
+};
+// Compile-time form of a marching launch. kMarchGeneric reads every stage
+// option from StageParams at run time; the two lean forms are the stages of
+// a problem without viscosity, SGS stress or drag (the inviscid runs) with
+// the RK combine's blend form fixed, so that the walk carries no viscous
+// window row and tests no per-launch flag in its steady state.
+enum MarchForm { kMarchGeneric = 0, kMarchLeanPlain = 1, kMarchLeanBlend = 2 };
 // Columns per lane of a marching tile width (0: not a marching width).
 inline int march_cols(int tile_x) {
   for (int nc = 1; nc <= 3; ++nc)
@@ -146,11 +159,11 @@ cudaError_t launch_march_ppm4(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_ppmx(int, int, const StageParams&, dim3, cudaStream_t);
 cudaError_t launch_march_wenoz(int, int, const StageParams&, dim3, cudaStream_t);
 // (dtype, rsolver, nv, nc, params, tile offsets, nsolves, nwork, grid, stream)
-cudaError_t launch_batch_march_dc(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_plm(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppm4(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_ppmx(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
-cudaError_t launch_batch_march_wenoz(int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_dc(int, int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_plm(int, int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppm4(int, int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_ppmx(int, int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
+cudaError_t launch_batch_march_wenoz(int, int, int, int, int, int, const StageParams*, const int*, int, int, dim3, cudaStream_t);
 int march_blocks_per_sm_dc(int dtype, int rsolver, int nv, int nc, int kind);
 int march_blocks_per_sm_plm(int dtype, int rsolver, int nv, int nc, int kind);
 int march_blocks_per_sm_ppm4(int dtype, int rsolver, int nv, int nc, int kind);

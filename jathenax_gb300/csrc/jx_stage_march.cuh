@@ -119,12 +119,6 @@ template <typename R> struct MarchColumn {
   Cell4<R> W4, W3, W2, W1, W0, Ay2, hy3, Fy3;
 };
 
-// Compile-time form of a marching launch. kMarchGeneric reads every stage
-// option from StageParams at run time; the two lean forms are the stages of
-// a problem without viscosity, SGS stress or drag (the inviscid runs) with
-// the RK combine's blend form fixed, so that the walk carries no viscous
-// window row and tests no per-launch flag in its steady state.
-enum MarchForm { kMarchGeneric = 0, kMarchLeanPlain = 1, kMarchLeanBlend = 2 };
 
 // The cell at column c0 + K of the lane's row, K in [-2, NC + 1]: one of
 // the lane's own NC columns, or a neighbouring lane's by a warp shuffle.
@@ -589,6 +583,28 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // only on request: its default is the shared-memory tile) always runs the
 // generic form with two columns per lane. One column per lane (a latency
 // choice for small grids) runs the generic form.
+// Batched packed-pair walk (see stage_kernel_batch_march): a launch group of
+// 4-variable lean solves with one integrator, so that every member's stage
+// has the same form.
+template <int RECON, int RS, int FORM, bool RING>
+__global__ void __launch_bounds__(32, RECON == JX_WENOZ ? 8 : 12) stage_kernel_batch_march_pk(
+    const StageParams* __restrict__ params, const int* __restrict__ tile_offset, int nsolves, int nwork) {
+  extern __shared__ float4 march_ring[];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    int lo = 0, hi = nsolves - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile_offset[mid] <= w) lo = mid;
+      else hi = mid - 1;
+    }
+    const StageParams& p = params[lo];
+    if (p.skip || p.clock->done) continue;
+    pk::march_tile_pk<RECON, RS, 4, FORM == kMarchLeanBlend, RING>(p, w - tile_offset[lo],
+                                                                   tile_offset[lo + 1] - tile_offset[lo],
+                                                                   RING ? march_ring : nullptr);
+  }
+}
+
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
@@ -679,9 +695,46 @@ cudaError_t launch_batch_march_rs_nv(int nc, bool ring, const StageParams* param
   return launch_batch_march_k<R, RECON, RS, NV, 2>(ring, params, offsets, nsolves, nwork, grid, s);
 }
 
+// A lean group's stage in the packed walk where march_packed allows it (the
+// same rules as the single-solve launches); true if launched.
+template <int RECON, int RS, int FORM>
+bool launch_batch_march_packed(bool ring, const StageParams* params, const int* offsets, int nsolves, int nwork,
+                               dim3 grid, cudaStream_t s) {
+  if constexpr (march_packed<float, RECON, RS, 4, 2, FORM>()) {
+    if (!ring) {
+      if constexpr (march_packed_short<RECON>()) {
+        stage_kernel_batch_march_pk<RECON, RS, FORM, false><<<grid, 32, 0, s>>>(params, offsets, nsolves, nwork);
+        return true;
+      }
+    } else if constexpr (march_packed_ring<RECON, RS>()) {
+      march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, FORM, true>>();
+      stage_kernel_batch_march_pk<RECON, RS, FORM, true><<<grid, 32, march_smem<2>(), s>>>(params, offsets, nsolves,
+                                                                                          nwork);
+      return true;
+    }
+  }
+  return false;
+}
+
+// Whether a lean group of (RECON, RS) at `ring` runs the packed walk.
 template <int RECON, int RS>
-cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
-                                  int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+bool batch_march_packed(bool ring) {
+  if constexpr (march_packed<float, RECON, RS, 4, 2, kMarchLeanBlend>())
+    return ring ? march_packed_ring<RECON, RS>() : march_packed_short<RECON>();
+  return false;
+}
+
+template <int RECON, int RS>
+cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, int ring, int form, const StageParams* params,
+                                  const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
+  if (dtype == JX_F32 && nv == 4 && nc == 2 && form != kMarchGeneric) {
+    const bool done = form == kMarchLeanBlend
+                          ? launch_batch_march_packed<RECON, RS, kMarchLeanBlend>(ring, params, offsets, nsolves, nwork,
+                                                                                grid, s)
+                          : launch_batch_march_packed<RECON, RS, kMarchLeanPlain>(ring, params, offsets, nsolves, nwork,
+                                                                                grid, s);
+    if (done) return cudaGetLastError();
+  }
   if (dtype == JX_F64)
     return nv == 3 ? launch_batch_march_rs_nv<double, RECON, RS, 3>(nc, ring, params, offsets, nsolves, nwork, grid, s)
                    : launch_batch_march_rs_nv<double, RECON, RS, 4>(nc, ring, params, offsets, nsolves, nwork, grid, s);
@@ -717,6 +770,19 @@ int march_single_occupancy() {
 
 template <typename R, int RECON, int RS, int NV, int NC>
 int march_blocks_per_sm_nv(int kind) {
+  if (kind == kMarchBatchPacked || kind == kMarchBatchPackedRing) {
+    if constexpr (march_packed<R, RECON, RS, NV, NC, kMarchLeanBlend>()) {
+      if (kind == kMarchBatchPackedRing) {
+        if constexpr (march_packed_ring<RECON, RS>()) {
+          march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, true>>();
+          return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, true>, march_smem<2>());
+        }
+      } else if constexpr (march_packed_short<RECON>()) {
+        return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, false>);
+      }
+    }
+    kind = kind == kMarchBatchPackedRing ? kMarchBatchRing : kMarchBatch;
+  }
   if (kind == kMarchBatch || kind == kMarchBatchRing) {
     if constexpr (march_ring_on<R, RECON, NC>()) {
       if (kind == kMarchBatchRing) {
@@ -747,6 +813,9 @@ int march_blocks_per_sm_rs(int nv, int nc, int kind) {
 
 template <int RECON, int RS>
 int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, int kind) {
+  if ((kind == kMarchBatchPacked || kind == kMarchBatchPackedRing) &&
+      !(dtype == JX_F32 && nv == 4 && nc == 2 && batch_march_packed<RECON, RS>(kind == kMarchBatchPackedRing)))
+    kind = kind == kMarchBatchPackedRing ? kMarchBatchRing : kMarchBatch;
   return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, kind)
                          : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, kind);
 }

@@ -6,15 +6,15 @@
 
 namespace jx {
 cudaError_t launch_march_plm_llf(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
-cudaError_t launch_batch_march_plm_llf(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_plm_llf(int dtype, int nv, int nc, int ring, int form, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
 int march_blocks_per_sm_plm_llf(int dtype, int nv, int nc, int kind);
 cudaError_t launch_march_plm_hlle(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
-cudaError_t launch_batch_march_plm_hlle(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_plm_hlle(int dtype, int nv, int nc, int ring, int form, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
 int march_blocks_per_sm_plm_hlle(int dtype, int nv, int nc, int kind);
 cudaError_t launch_march_plm_roe(int dtype, const StageParams& p, dim3 grid, cudaStream_t s);
-cudaError_t launch_batch_march_plm_roe(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_plm_roe(int dtype, int nv, int nc, int ring, int form, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s);
 int march_blocks_per_sm_plm_roe(int dtype, int nv, int nc, int kind);
 
@@ -26,12 +26,12 @@ cudaError_t launch_march_plm(int dtype, int rsolver, const StageParams& p, dim3 
   }
   return cudaErrorInvalidValue;
 }
-cudaError_t launch_batch_march_plm(int dtype, int rsolver, int nv, int nc, int ring, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_plm(int dtype, int rsolver, int nv, int nc, int ring, int form, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
   switch (rsolver) {
-    case JX_LLF: return launch_batch_march_plm_llf(dtype, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    case JX_HLLE: return launch_batch_march_plm_hlle(dtype, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
-    case JX_ROE: return launch_batch_march_plm_roe(dtype, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+    case JX_LLF: return launch_batch_march_plm_llf(dtype, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    case JX_HLLE: return launch_batch_march_plm_hlle(dtype, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
+    case JX_ROE: return launch_batch_march_plm_roe(dtype, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
   }
   return cudaErrorInvalidValue;
 }

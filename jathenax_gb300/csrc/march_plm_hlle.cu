@@ -6,9 +6,9 @@ namespace jx {
 cudaError_t launch_march_plm_hlle(int dtype, const StageParams& p, dim3 grid, cudaStream_t s) {
   return launch_march_rs<JX_PLM, JX_HLLE>(dtype, p, grid, s);
 }
-cudaError_t launch_batch_march_plm_hlle(int dtype, int nv, int nc, int ring, const StageParams* params, const int* offsets,
+cudaError_t launch_batch_march_plm_hlle(int dtype, int nv, int nc, int ring, int form, const StageParams* params, const int* offsets,
                                   int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  return launch_batch_march_rs<JX_PLM, JX_HLLE>(dtype, nv, nc, ring, params, offsets, nsolves, nwork, grid, s);
+  return launch_batch_march_rs<JX_PLM, JX_HLLE>(dtype, nv, nc, ring, form, params, offsets, nsolves, nwork, grid, s);
 }
 int march_blocks_per_sm_plm_hlle(int dtype, int nv, int nc, int kind) {
   return march_blocks_per_sm_rs_dtype<JX_PLM, JX_HLLE>(dtype, nv, nc, kind);

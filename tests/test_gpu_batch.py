@@ -144,3 +144,26 @@ def test_float32_batch_mixing_methods_and_columns_per_lane_is_bitwise():
         c = s.state()
         assert (c.time, c.cycle) == (t_alone, cyc_alone), (k, c.time, t_alone)
         np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=f"solve {k}")
+
+
+def test_lean_four_variable_groups_are_bitwise_solo():
+    """Inviscid 4-variable float32 solves on two-column marching tiles form
+    lean groups per integrator, which run the packed-pair walk where it is
+    used (short tiles, and tall ones with the row ring): each result is
+    bitwise its solo run."""
+    from jathenax_gb300.batch import Batch, ClockBank
+    specs = [("kh", 70, "float32", "ppm4", "roe", "rk3", 0.03), ("kh", 64, "float32", "ppm4", "llf", "rk2", 0.03),
+             ("kh", 60, "float32", "plm", "hlle", "rk4", 0.02), ("kh", 66, "float32", "wenoz", "hlle", "rk3", 0.02),
+             ("kh", 58, "float32", "ppm4", "roe", "rk4", 0.02), ("kh", 50, "float32", "ppm4", "hlle", "rk3", 0.03)]
+    tiles = [(58, 16), (58, 32)]
+    bank = ClockBank(len(specs) * len(tiles))
+    solves, expect = [], []
+    for i, spec in enumerate(specs):
+        for j, (tx, ty) in enumerate(tiles):
+            solves.append(make_solve(*spec, tile_y=ty, tile_x=tx, clock=bank.slot(i * len(tiles) + j)))
+            expect.append(run_alone(spec, ty, tx))
+    Batch(solves, clocks=bank).run(steps_per_sync=4)
+    for k, (s, (U_alone, t_alone, cyc_alone)) in enumerate(zip(solves, expect)):
+        c = s.state()
+        assert (c.time, c.cycle) == (t_alone, cyc_alone), (k, c.time, t_alone)
+        np.testing.assert_array_equal(s.S.cpu().numpy(), U_alone, err_msg=f"solve {k}")
