@@ -508,30 +508,32 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, 
 
 template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
 
-// PLM, PPM4 and WENO-Z with 4 variables in a lean form with two columns per
-// lane run the packed-pair walk of jx_stage_march_pk.cuh (float32) where it
-// measured faster than the per-column walk (GB300, RK3 stage 2):
+// PLM, PPM4, PPMX and WENO-Z with 4 variables in a lean form with two
+// columns per lane run the packed-pair walk of jx_stage_march_pk.cuh
+// (float32) where it measured faster than the per-column walk (GB300, RK3
+// stage 2):
 //   * PPM4/Roe 0.2812 -> 0.2642 ms at 4096² (58 x 121, with the row ring),
 //     0.0269 -> 0.0249 ms at 1024² (58 x 8); HLLE 0.2886 -> 0.2717 and
 //     0.0270 -> 0.0250 ms; LLF 0.0221 -> 0.0208 ms at 1024², but its ring
 //     kernel spills (0.2437 -> 0.2618 ms), so LLF's tall tiles keep the
 //     per-column ring walk;
 //   * PLM/HLLE 0.3466 -> 0.3259 ms at 4096², 0.0311 -> 0.0290 ms at 1024²;
+//   * PPMX/Roe 0.6559 -> 0.6014 and 0.0577 -> 0.0535 ms; LLF 0.5699 ->
+//     0.5467 and 0.0518 -> 0.0496 ms;
 //   * WENO-Z/HLLE on 58 x 121 tiles 1.481 -> 1.344 ms, but on the 8-row
 //     tiles of a 1024² grid 0.123 -> 0.156 ms, so only tall tiles use it
 //     (WENO-Z defaults to one column per lane, which it does not cover);
 //   * DC: 0.176 -> 0.202 ms at 4096², 0.0144 ms either way at 1024²: not used.
 // With 3 variables PPM4 measured 1 % slower (0.2379 -> 0.2404 ms): not used.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
-  return sizeof(R) == 4 && (RECON == JX_PLM || RECON == JX_PPM4 || RECON == JX_WENOZ) && NV == 4 && NC == 2 &&
-         FORM != kMarchGeneric;
+  return sizeof(R) == 4 && RECON != JX_DC && NV == 4 && NC == 2 && FORM != kMarchGeneric;
 }
 template <int RECON> constexpr bool march_packed_short() { return RECON != JX_WENOZ; }
 template <int RECON, int RS> constexpr bool march_packed_ring() { return RECON != JX_PPM4 || RS != JX_LLF; }
 
 static_assert(kMarchWarps == 1, "the packed-pair kernel takes one tile per single-warp block");
 template <int RECON, int RS, int NV, int FORM, bool RING>
-__global__ void __launch_bounds__(32, RECON == JX_WENOZ ? 12 : 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
+__global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 12 : 16) stage_kernel_march_pk(const StageParams p, int ntiles) {
   if (p.clock->done) return;
   const int tile = blockIdx.x;
   if (tile >= ntiles) return;
@@ -587,7 +589,7 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // 4-variable lean solves with one integrator, so that every member's stage
 // has the same form.
 template <int RECON, int RS, int FORM, bool RING>
-__global__ void __launch_bounds__(32, RECON == JX_WENOZ ? 8 : 12) stage_kernel_batch_march_pk(
+__global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 8 : 12) stage_kernel_batch_march_pk(
     const StageParams* __restrict__ params, const int* __restrict__ tile_offset, int nsolves, int nwork) {
   extern __shared__ float4 march_ring[];
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {

@@ -1,4 +1,4 @@
-// Float32 marching stage (DC, PLM, PPM4 or WENO-Z edges, any Riemann solver,
+// Float32 marching stage (DC, PLM, PPM4, PPMX or WENO-Z edges, any Riemann solver,
 // the inviscid "lean" forms, 3 or 4 variables, two columns per lane) with the
 // lane's two columns held as float32 pairs. Which (reconstruction, solver,
 // variables, tile) combinations use it is decided by measurement; see
@@ -211,12 +211,65 @@ __device__ __forceinline__ PCell face_flux2(const PCell& L, const PCell& Rv, con
   return f;
 }
 
-template <int NV>
-__device__ __forceinline__ PCell faces2(const PCell& w0, const PCell& w1, const PCell& w2, const PCell& w3) {
-  PCell a;
-#pragma unroll
-  for (int v = 0; v < 4; ++v) a.v[v] = v < NV ? ppm4_face2(w0.v[v], w1.v[v], w2.v[v], w3.v[v]) : splat(0.f);
-  return a;
+
+// -(c ? a : 0) per half (a negative zero where c is false, as the scalar form).
+__device__ __forceinline__ F2 neg_if(bool cx, bool cy, F2 a) { return make_float2(-(cx ? a.x : 0.f), -(cy ? a.y : 0.f)); }
+
+// ppmx_edge (float32) for both halves: the smooth-extremum limiter of one
+// face value (fluxes.py:45-53).
+__device__ __forceinline__ F2 ppmx_edge2(F2 a, F2 b, F2 edge, F2 ca, F2 cb) {
+  using N = Num<float>;
+  const F2 curv = mul(splat(3.f), fma(splat(-2.f), edge, add(a, b)));
+  const bool ax = (curv.x > 0.f && ca.x > 0.f && cb.x > 0.f) || (curv.x < 0.f && ca.x < 0.f && cb.x < 0.f);
+  const bool ay = (curv.y > 0.f && ca.y > 0.f && cb.y > 0.f) || (curv.y < 0.f && ca.y < 0.f && cb.y < 0.f);
+  const F2 mag = make_float2(N::pmin(fabsf(ca.x), fabsf(cb.x)), N::pmin(fabsf(ca.y), fabsf(cb.y)));
+  const F2 m125 = mul(splat(1.25f), mag);
+  const F2 lim = make_float2(copysignf(N::pmin(m125.x, fabsf(curv.x)), curv.x),
+                             copysignf(N::pmin(m125.y, fabsf(curv.y)), curv.y));
+  const F2 fixed = fma(neg_if(ax, ay, lim), splat(float(1.0 / 6.0)), mul(splat(0.5f), add(a, b)));
+  const F2 p = mul(sub(a, edge), sub(b, edge));
+  return sel(p.x > 0.f, p.y > 0.f, fixed, edge);
+}
+
+// ppmx_face (float32) for both halves (fluxes.py:62-68).
+__device__ __forceinline__ F2 ppmx_face2(F2 w0, F2 w1, F2 w2, F2 w3) {
+  const F2 e = mul(fma(splat(7.f), add(w2, w1), neg(add(w0, w3))), splat(float(1.0 / 12.0)));
+  const F2 c1 = fma(splat(-2.f), w1, add(w0, w2));
+  const F2 c2 = fma(splat(-2.f), w2, add(w1, w3));
+  return ppmx_edge2(w1, w2, e, c1, c2);
+}
+
+// ppmx_cell (float32 branch) for both halves (fluxes.py:70-84).
+__device__ __forceinline__ void ppmx_cell2(F2 m2, F2 m1, F2 c, F2 p1, F2 p2, F2 lo_face, F2 hi_face, F2& lo, F2& hi) {
+  using N = Num<float>;
+  const F2 cl = fma(splat(-2.f), m1, add(m2, c));
+  const F2 cm = fma(splat(-2.f), c, add(m1, p1));
+  const F2 cr = fma(splat(-2.f), p1, add(c, p2));
+  const F2 dh = sub(hi_face, c);
+  const F2 dl = sub(lo_face, c);
+  const F2 e1 = mul(dh, sub(c, lo_face)), e2 = mul(sub(m1, c), sub(c, p1));
+  const bool ext_x = e1.x <= 0.f || e2.x <= 0.f, ext_y = e1.y <= 0.f || e2.y <= 0.f;
+  const F2 d2 = mul(splat(6.f), fma(splat(-2.f), c, add(lo_face, hi_face)));
+  const bool ag_x = (d2.x > 0.f && cl.x > 0.f && cm.x > 0.f && cr.x > 0.f) ||
+                    (d2.x < 0.f && cl.x < 0.f && cm.x < 0.f && cr.x < 0.f);
+  const bool ag_y = (d2.y > 0.f && cl.y > 0.f && cm.y > 0.f && cr.y > 0.f) ||
+                    (d2.y < 0.f && cl.y < 0.f && cm.y < 0.f && cr.y < 0.f);
+  const F2 mag = make_float2(N::pmin(fabsf(cm.x), N::pmin(fabsf(cl.x), fabsf(cr.x))),
+                             N::pmin(fabsf(cm.y), N::pmin(fabsf(cl.y), fabsf(cr.y))));
+  const F2 m125 = mul(splat(1.25f), mag);
+  const F2 lim = make_float2(copysignf(N::pmin(m125.x, fabsf(d2.x)), d2.x),
+                             copysignf(N::pmin(m125.y, fabsf(d2.y)), d2.y));
+  const F2 scale = make_float2(N::pmax(fabsf(m1.x), N::pmax(fabsf(c.x), fabsf(p1.x))),
+                               N::pmax(fabsf(m1.y), N::pmax(fabsf(c.y), fabsf(p1.y))));
+  const F2 thr = mul(splat(float(1e-12)), scale);
+  const bool use_x = ag_x && fabsf(d2.x) > thr.x, use_y = ag_y && fabsf(d2.y) > thr.y;
+  const F2 ratio = make_float2(use_x ? N::quick_div(lim.x, d2.x) : 0.f, use_y ? N::quick_div(lim.y, d2.y) : 0.f);
+  const bool slo_x = fabsf(dl.x) >= 2.f * fabsf(dh.x), slo_y = fabsf(dl.y) >= 2.f * fabsf(dh.y);
+  const bool shi_x = fabsf(dh.x) >= 2.f * fabsf(dl.x), shi_y = fabsf(dh.y) >= 2.f * fabsf(dl.y);
+  const F2 lm = sel(slo_x, slo_y, fma(splat(-2.f), dh, c), lo_face);
+  const F2 hm = sel(shi_x, shi_y, fma(splat(-2.f), dl, c), hi_face);
+  lo = sel(ext_x, ext_y, fma(dl, ratio, c), lm);
+  hi = sel(ext_x, ext_y, fma(dh, ratio, c), hm);
 }
 
 __device__ __forceinline__ F2 div2(F2 a, F2 b) { return make_float2(Num<float>::div(a.x, b.x), Num<float>::div(a.y, b.y)); }
@@ -264,6 +317,18 @@ __device__ __forceinline__ void wenoz_cell2(F2 m2, F2 m1, F2 c, F2 p1, F2 p2, F2
   lo = wenoz_combine2(p2, p1, c, m1, m2, w2, w1, w0);
 }
 
+template <int RECON, int NV>
+__device__ __forceinline__ PCell faces2(const PCell& w0, const PCell& w1, const PCell& w2, const PCell& w3) {
+  PCell a;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    if (v >= NV) a.v[v] = splat(0.f);
+    else if constexpr (RECON == JX_PPM4) a.v[v] = ppm4_face2(w0.v[v], w1.v[v], w2.v[v], w3.v[v]);
+    else a.v[v] = ppmx_face2(w0.v[v], w1.v[v], w2.v[v], w3.v[v]);
+  }
+  return a;
+}
+
 // edges_cells for both halves: the low/high edges of the cells at the
 // centre of (m2, m1, c, p1, p2); lf/hf the face values (PPM4 only).
 template <int RECON, int NV>
@@ -279,6 +344,8 @@ __device__ __forceinline__ void edges2(const PCell& m2, const PCell& m1, const P
         plm_cell2(m1.v[v], c.v[v], p1.v[v], lo.v[v], hi.v[v]);
       } else if constexpr (RECON == JX_PPM4) {
         ppm4_cell2(c.v[v], lf.v[v], hf.v[v], lo.v[v], hi.v[v]);
+      } else if constexpr (RECON == JX_PPMX) {
+        ppmx_cell2(m2.v[v], m1.v[v], c.v[v], p1.v[v], p2.v[v], lf.v[v], hf.v[v], lo.v[v], hi.v[v]);
       } else {
         wenoz_cell2(m2.v[v], m1.v[v], c.v[v], p1.v[v], p2.v[v], lo.v[v], hi.v[v]);
       }
@@ -286,7 +353,7 @@ __device__ __forceinline__ void edges2(const PCell& m2, const PCell& m1, const P
       lo.v[v] = hi.v[v] = splat(0.f);
     }
   }
-  if constexpr (RECON == JX_WENOZ) {  // fluxes.py:128-130
+  if constexpr (RECON == JX_PPMX || RECON == JX_WENOZ) {  // fluxes.py:128-130
     lo.v[0] = max2(lo.v[0], splat(dfloor));
     hi.v[0] = max2(hi.v[0], splat(dfloor));
   }
@@ -402,8 +469,8 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
     }
     // ---- y sweep of both columns -------------------------------------------
     PCell Ay1 = c.Ay2;
-    if constexpr (RECON == JX_PPM4)
-      if (kSteady || it >= 3) Ay1 = faces2<NV>(c.W3, c.W2, c.W1, c.W0);
+    if constexpr (RECON == JX_PPM4 || RECON == JX_PPMX)
+      if (kSteady || it >= 3) Ay1 = faces2<RECON, NV>(c.W3, c.W2, c.W1, c.W0);
     PCell lo = c.hy3, hi = c.hy3;
     if (kSteady || it >= 4) edges2<RECON, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1, k.dfloor, lo, hi);
     PCell Fy2 = c.Fy3;
@@ -416,8 +483,8 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
       const PCell m1 = straddle<NV>(L, own);             // (c0-1, c0)
       const PCell p1 = straddle<NV>(own, R);             // (c0+1, c0+2)
       PCell lf = own, hf = own;
-      if constexpr (RECON == JX_PPM4) {
-        lf = faces2<NV>(L, m1, own, p1);  // faces c0, c0+1
+      if constexpr (RECON == JX_PPM4 || RECON == JX_PPMX) {
+        lf = faces2<RECON, NV>(L, m1, own, p1);  // faces c0, c0+1
         float A2[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) A2[v] = v < NV ? __shfl_down_sync(0xffffffffu, lf.v[v].x, 1) : 0.f;  // face c0+2
