@@ -508,10 +508,10 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_min_blocks<R, RECON, 
 
 template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_bytes<NC>() * kMarchWarps; }
 
-// PLM, PPM4, PPMX and WENO-Z with 4 variables in a lean form with two
-// columns per lane run the packed-pair walk of jx_stage_march_pk.cuh
-// (float32) where it measured faster than the per-column walk (GB300, RK3
-// stage 2):
+// PLM, PPM4, PPMX and WENO-Z with two columns per lane run the packed-pair
+// walk of jx_stage_march_pk.cuh (float32) where it measured faster than the
+// per-column walk (GB300, RK3 stage 2): 4 variables in the lean forms and 3
+// in the generic form.
 //   * PPM4/Roe 0.2812 -> 0.2642 ms at 4096² (58 x 121, with the row ring),
 //     0.0269 -> 0.0249 ms at 1024² (58 x 8); HLLE 0.2886 -> 0.2717 and
 //     0.0270 -> 0.0250 ms; LLF 0.0221 -> 0.0208 ms at 1024², but its ring
@@ -523,10 +523,14 @@ template <int NC> constexpr size_t march_smem() { return (size_t)march_ring_byte
 //   * WENO-Z/HLLE on 58 x 121 tiles 1.481 -> 1.344 ms, but on the 8-row
 //     tiles of a 1024² grid 0.123 -> 0.156 ms, so only tall tiles use it
 //     (WENO-Z defaults to one column per lane, which it does not cover);
-//   * DC: 0.176 -> 0.202 ms at 4096², 0.0144 ms either way at 1024²: not used.
-// With 3 variables PPM4 measured 1 % slower (0.2379 -> 0.2404 ms): not used.
+//   * DC: 0.176 -> 0.202 ms at 4096², 0.0144 ms either way at 1024²: not used;
+//   * 3 variables, lean: PPM4 1 % slower (0.2379 -> 0.2404 ms): not used;
+//     3 variables, generic form (viscosity and drag): PPM4/Roe 0.2944 ->
+//     0.2704 ms at 4096², 0.0270 -> 0.0249 ms at 1024², PLM/HLLE 0.3597 ->
+//     0.3262 ms: used (not with SGS stress, which has no packed path);
+//   * 4 variables, generic form: the kernel spills at 16 warps; not used.
 template <typename R, int RECON, int RS, int NV, int NC, int FORM> constexpr bool march_packed() {
-  return sizeof(R) == 4 && RECON != JX_DC && NV == 4 && NC == 2 && FORM != kMarchGeneric;
+  return sizeof(R) == 4 && RECON != JX_DC && NC == 2 && (NV == 4 ? FORM != kMarchGeneric : FORM == kMarchGeneric);
 }
 template <int RECON> constexpr bool march_packed_short() { return RECON != JX_WENOZ; }
 template <int RECON, int RS> constexpr bool march_packed_ring() { return RECON != JX_PPM4 || RS != JX_LLF; }
@@ -538,7 +542,7 @@ __global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 12 : 16) stage_kernel_m
   const int tile = blockIdx.x;
   if (tile >= ntiles) return;
   extern __shared__ float4 march_ring[];
-  pk::march_tile_pk<RECON, RS, NV, FORM == kMarchLeanBlend, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
+  pk::march_tile_pk<RECON, RS, NV, FORM, RING>(p, tile, ntiles, RING ? march_ring : nullptr);
 }
 
 // Let a ring kernel have the largest shared-memory carve-out (once per kernel).
@@ -587,8 +591,8 @@ __global__ void __launch_bounds__(kMarchWarps * 32, (march_batch_min_blocks<R, R
 // choice for small grids) runs the generic form.
 // Batched packed-pair walk (see stage_kernel_batch_march): a launch group of
 // 4-variable lean solves with one integrator, so that every member's stage
-// has the same form.
-template <int RECON, int RS, int FORM, bool RING>
+// has the same form, or of 3-variable solves in the generic form.
+template <int RECON, int RS, int NV, int FORM, bool RING>
 __global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 8 : 12) stage_kernel_batch_march_pk(
     const StageParams* __restrict__ params, const int* __restrict__ tile_offset, int nsolves, int nwork) {
   extern __shared__ float4 march_ring[];
@@ -601,7 +605,7 @@ __global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 8 : 12) stage_kernel_ba
     }
     const StageParams& p = params[lo];
     if (p.skip || p.clock->done) continue;
-    pk::march_tile_pk<RECON, RS, 4, FORM == kMarchLeanBlend, RING>(p, w - tile_offset[lo],
+    pk::march_tile_pk<RECON, RS, NV, FORM, RING>(p, w - tile_offset[lo],
                                                                    tile_offset[lo + 1] - tile_offset[lo],
                                                                    RING ? march_ring : nullptr);
   }
@@ -610,7 +614,9 @@ __global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 8 : 12) stage_kernel_ba
 template <typename R, int RECON, int RS, int NV, int NC, int FORM>
 cudaError_t launch_march_form(const StageParams& p, dim3 blocks, dim3 threads, int ntiles, cudaStream_t s) {
   if constexpr (march_packed<R, RECON, RS, NV, NC, FORM>()) {
-    if (p.ty < kRingMinRows) {
+    if (FORM == kMarchGeneric && p.tau) {
+      // SGS stress: the per-column walk (the packed one has no stress path).
+    } else if (p.ty < kRingMinRows) {
       if constexpr (march_packed_short<RECON>()) {
         stage_kernel_march_pk<RECON, RS, NV, FORM, false><<<blocks, threads, 0, s>>>(p, ntiles);
         return cudaGetLastError();
@@ -697,31 +703,32 @@ cudaError_t launch_batch_march_rs_nv(int nc, bool ring, const StageParams* param
   return launch_batch_march_k<R, RECON, RS, NV, 2>(ring, params, offsets, nsolves, nwork, grid, s);
 }
 
-// A lean group's stage in the packed walk where march_packed allows it (the
-// same rules as the single-solve launches); true if launched.
-template <int RECON, int RS, int FORM>
+// A group's stage in the packed walk where march_packed allows it (the same
+// rules as the single-solve launches; batches carry no SGS stress); true if
+// launched.
+template <int RECON, int RS, int NV, int FORM>
 bool launch_batch_march_packed(bool ring, const StageParams* params, const int* offsets, int nsolves, int nwork,
                                dim3 grid, cudaStream_t s) {
-  if constexpr (march_packed<float, RECON, RS, 4, 2, FORM>()) {
+  if constexpr (march_packed<float, RECON, RS, NV, 2, FORM>()) {
     if (!ring) {
       if constexpr (march_packed_short<RECON>()) {
-        stage_kernel_batch_march_pk<RECON, RS, FORM, false><<<grid, 32, 0, s>>>(params, offsets, nsolves, nwork);
+        stage_kernel_batch_march_pk<RECON, RS, NV, FORM, false><<<grid, 32, 0, s>>>(params, offsets, nsolves, nwork);
         return true;
       }
     } else if constexpr (march_packed_ring<RECON, RS>()) {
-      march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, FORM, true>>();
-      stage_kernel_batch_march_pk<RECON, RS, FORM, true><<<grid, 32, march_smem<2>(), s>>>(params, offsets, nsolves,
-                                                                                          nwork);
+      march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, NV, FORM, true>>();
+      stage_kernel_batch_march_pk<RECON, RS, NV, FORM, true><<<grid, 32, march_smem<2>(), s>>>(params, offsets,
+                                                                                              nsolves, nwork);
       return true;
     }
   }
   return false;
 }
 
-// Whether a lean group of (RECON, RS) at `ring` runs the packed walk.
-template <int RECON, int RS>
+// Whether a group of (RECON, RS, NV, FORM) at `ring` runs the packed walk.
+template <int RECON, int RS, int NV, int FORM>
 bool batch_march_packed(bool ring) {
-  if constexpr (march_packed<float, RECON, RS, 4, 2, kMarchLeanBlend>())
+  if constexpr (march_packed<float, RECON, RS, NV, 2, FORM>())
     return ring ? march_packed_ring<RECON, RS>() : march_packed_short<RECON>();
   return false;
 }
@@ -729,12 +736,14 @@ bool batch_march_packed(bool ring) {
 template <int RECON, int RS>
 cudaError_t launch_batch_march_rs(int dtype, int nv, int nc, int ring, int form, const StageParams* params,
                                   const int* offsets, int nsolves, int nwork, dim3 grid, cudaStream_t s) {
-  if (dtype == JX_F32 && nv == 4 && nc == 2 && form != kMarchGeneric) {
-    const bool done = form == kMarchLeanBlend
-                          ? launch_batch_march_packed<RECON, RS, kMarchLeanBlend>(ring, params, offsets, nsolves, nwork,
-                                                                                grid, s)
-                          : launch_batch_march_packed<RECON, RS, kMarchLeanPlain>(ring, params, offsets, nsolves, nwork,
-                                                                                grid, s);
+  if (dtype == JX_F32 && nc == 2) {
+    bool done = false;
+    if (nv == 4 && form == kMarchLeanBlend)
+      done = launch_batch_march_packed<RECON, RS, 4, kMarchLeanBlend>(ring, params, offsets, nsolves, nwork, grid, s);
+    else if (nv == 4 && form == kMarchLeanPlain)
+      done = launch_batch_march_packed<RECON, RS, 4, kMarchLeanPlain>(ring, params, offsets, nsolves, nwork, grid, s);
+    else if (nv == 3 && form == kMarchGeneric)
+      done = launch_batch_march_packed<RECON, RS, 3, kMarchGeneric>(ring, params, offsets, nsolves, nwork, grid, s);
     if (done) return cudaGetLastError();
   }
   if (dtype == JX_F64)
@@ -770,20 +779,34 @@ int march_single_occupancy() {
   return march_occupancy(stage_kernel_march<R, RECON, RS, NV, NC, FORM>);
 }
 
+// Resident blocks of the batched packed kernel of FORM, or 0 where the
+// packed walk does not run.
+template <typename R, int RECON, int RS, int NV, int NC, int FORM>
+int batch_packed_occupancy(bool ring) {
+  if constexpr (sizeof(R) == 4 && NC == 2 && march_packed<R, RECON, RS, NV, NC, FORM>()) {
+    if (ring) {
+      if constexpr (march_packed_ring<RECON, RS>()) {
+        march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, NV, FORM, true>>();
+        return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, NV, FORM, true>, march_smem<2>());
+      }
+    } else if constexpr (march_packed_short<RECON>()) {
+      return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, NV, FORM, false>);
+    }
+  }
+  return 0;
+}
+
 template <typename R, int RECON, int RS, int NV, int NC>
 int march_blocks_per_sm_nv(int kind) {
   if (kind == kMarchBatchPacked || kind == kMarchBatchPackedRing) {
-    if constexpr (march_packed<R, RECON, RS, NV, NC, kMarchLeanBlend>()) {
-      if (kind == kMarchBatchPackedRing) {
-        if constexpr (march_packed_ring<RECON, RS>()) {
-          march_prefer_shared<stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, true>>();
-          return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, true>, march_smem<2>());
-        }
-      } else if constexpr (march_packed_short<RECON>()) {
-        return march_occupancy(stage_kernel_batch_march_pk<RECON, RS, kMarchLeanBlend, false>);
-      }
-    }
+    const int n = batch_packed_occupancy<R, RECON, RS, NV, NC, kMarchLeanBlend>(kind == kMarchBatchPackedRing);
+    if (n > 0) return n;
     kind = kind == kMarchBatchPackedRing ? kMarchBatchRing : kMarchBatch;
+  }
+  if (kind == kMarchBatch || kind == kMarchBatchRing) {
+    // Generic groups of 3-variable solves run the packed walk where it is used.
+    const int n = batch_packed_occupancy<R, RECON, RS, NV, NC, kMarchGeneric>(kind == kMarchBatchRing);
+    if (n > 0) return n;
   }
   if (kind == kMarchBatch || kind == kMarchBatchRing) {
     if constexpr (march_ring_on<R, RECON, NC>()) {
@@ -816,7 +839,8 @@ int march_blocks_per_sm_rs(int nv, int nc, int kind) {
 template <int RECON, int RS>
 int march_blocks_per_sm_rs_dtype(int dtype, int nv, int nc, int kind) {
   if ((kind == kMarchBatchPacked || kind == kMarchBatchPackedRing) &&
-      !(dtype == JX_F32 && nv == 4 && nc == 2 && batch_march_packed<RECON, RS>(kind == kMarchBatchPackedRing)))
+      !(dtype == JX_F32 && nv == 4 && nc == 2 &&
+        batch_march_packed<RECON, RS, 4, kMarchLeanBlend>(kind == kMarchBatchPackedRing)))
     kind = kind == kMarchBatchPackedRing ? kMarchBatchRing : kMarchBatch;
   return dtype == JX_F64 ? march_blocks_per_sm_rs<double, RECON, RS>(nv, nc, kind)
                          : march_blocks_per_sm_rs<float, RECON, RS>(nv, nc, kind);

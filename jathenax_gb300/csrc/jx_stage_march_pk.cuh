@@ -373,6 +373,32 @@ __device__ __forceinline__ PCell recover2(const Cell4<float>& a, const Cell4<flo
   return w;
 }
 
+// viscous_face (float32 branch) for both halves (fluxes.py:227-266): the
+// momentum flux of the face between cells a (low side) and b (high side)
+// from their velocities and the transverse sums (tp: columns or rows on the
+// high side, tm: on the low side).
+template <int DIR>
+__device__ __forceinline__ void viscous_face2(bool smag, float nu0, float smag_c, float inv_dn, float inv_4dt,
+                                              F2 rho_a, F2 rho_b, F2 ax, F2 ay, F2 bx, F2 by, F2 tpx, F2 tpy,
+                                              F2 tmx, F2 tmy, F2& f1, F2& f2) {
+  const F2 dn_x = mul(sub(bx, ax), splat(inv_dn)), dn_y = mul(sub(by, ay), splat(inv_dn));
+  const F2 dt_x = mul(sub(tpx, tmx), splat(inv_4dt)), dt_y = mul(sub(tpy, tmy), splat(inv_4dt));
+  const F2 dvx_dx = DIR == 0 ? dn_x : dt_x, dvy_dx = DIR == 0 ? dn_y : dt_y;
+  const F2 dvx_dy = DIR == 0 ? dt_x : dn_x, dvy_dy = DIR == 0 ? dt_y : dn_y;
+  const F2 shear = add(dvy_dx, dvx_dy);
+  const F2 k43 = splat(float(4.0 / 3.0)), k23 = splat(float(2.0 / 3.0));
+  const F2 s0 = DIR == 0 ? fma(k43, dvx_dx, neg(mul(k23, dvy_dy))) : shear;
+  const F2 s1 = DIR == 0 ? shear : fma(k43, dvy_dy, neg(mul(k23, dvx_dx)));
+  F2 nu = splat(nu0);
+  if (smag) {
+    const F2 s2 = fma(shear, shear, mul(splat(2.f), fma(dvx_dx, dvx_dx, mul(dvy_dy, dvy_dy))));
+    nu = fma(splat(smag_c), make_float2(sqrtf(s2.x), sqrtf(s2.y)), nu);
+  }
+  const F2 mu = neg(mul(mul(splat(0.5f), nu), add(rho_b, rho_a)));
+  f1 = fma(mu, s0, f1);
+  f2 = fma(mu, s1, f2);
+}
+
 // The lane's columns: the primitives of rows j-4 .. j (only WENO-Z reads
 // row j-4), the face value below row j-1 (PPM4), the upper edge of row j-3
 // and the y flux below row j-3.
@@ -383,7 +409,10 @@ struct ColumnPair {
 // One tile of kMarchTileX (58) columns by p.ty rows, one warp, two columns
 // per lane (lane l: columns c0 = x0 - 3 + 2 l and c0 + 1), as march_tile in
 // jx_stage_march.cuh walks it, with the same row ring when RING.
-template <int RECON, int RS, int NV, bool BLEND, bool RING>
+// FORM: 0 = generic (viscosity, Smagorinsky, drag and the blend flag read at
+// run time; no SGS stress), 1 = lean plain, 2 = lean blend (the MarchForm
+// values).
+template <int RECON, int RS, int NV, int FORM, bool RING>
 __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, int ntiles, float4* ring) {
   using N = Num<float>;
   const StageConsts<float>& k = stage_consts<float>(p);
@@ -415,6 +444,12 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
   gas.quarter_inv_cs = 0.5f * k.half_inv_cs;
   const float sdt = static_cast<float>(p.beta * p.clock->dt);
   const float ncx = -(sdt * k.inv_dx), ncy = -(sdt * k.inv_dy);
+  constexpr bool kLean = FORM != 0;
+  const bool visc = !kLean && p.visc_on;
+  const bool drag = !kLean && p.drag_on;
+  const bool blend = kLean ? FORM == 2 : (bool)p.blend;
+  const float kdrag = sdt * k.drag;
+  constexpr unsigned kAll = 0xffffffffu;
 
   ColumnPair c;
   c.W4 = c.W3 = c.W2 = c.W1 = c.W0 = c.Ay2 = c.hy3 = c.Fy3 = PCell{};
@@ -474,7 +509,19 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
     PCell lo = c.hy3, hi = c.hy3;
     if (kSteady || it >= 4) edges2<RECON, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1, k.dfloor, lo, hi);
     PCell Fy2 = c.Fy3;
-    if (kSteady || it >= 5) Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
+    if (kSteady || it >= 5) {
+      Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
+      if (visc) {
+        // Transverse x sums (row j-2 + row j-3) at the columns either side;
+        // a neighbour lane's sum is the same number it formed itself.
+        const F2 Sx = add(c.W2.v[1], c.W3.v[1]), Sy = add(c.W2.v[2], c.W3.v[2]);
+        const float sxm = __shfl_up_sync(kAll, Sx.y, 1), sym = __shfl_up_sync(kAll, Sy.y, 1);      // column c0-1
+        const float sxp = __shfl_down_sync(kAll, Sx.x, 1), syp = __shfl_down_sync(kAll, Sy.x, 1);  // column c0+2
+        viscous_face2<1>(p.smag_on, k.nu, k.smag_c, k.inv_dy, k.inv_4dx, c.W3.v[0], c.W2.v[0], c.W3.v[1], c.W3.v[2],
+                         c.W2.v[1], c.W2.v[2], make_float2(Sx.y, sxp), make_float2(Sy.y, syp),
+                         make_float2(sxm, Sx.x), make_float2(sym, Sy.x), Fy2.v[1], Fy2.v[2]);
+      }
+    }
     if (kSteady) {
       // ---- x sweep of row r = j-3 across the lanes -------------------------
       const PCell& own = c.W3;                           // columns (c0, c0+1)
@@ -495,7 +542,16 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
       edges2<RECON, NV>(L, m1, own, p1, R, lf, hf, k.dfloor, lx, hx);
 #pragma unroll
       for (int v = 0; v < 4; ++v) hiL[v] = v < NV ? __shfl_up_sync(0xffffffffu, hx.v[v].y, 1) : 0.f;  // column c0-1
-      const PCell F01 = face_flux2<RS, 0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
+      PCell F01 = face_flux2<RS, 0, NV>(straddle<NV>(hiL, hx), lx, gas);  // fluxes at faces c0, c0+1
+      if (visc) {
+        // Transverse y sums at the faces' two columns: rows r+1 (W2) and r-1 (W4).
+        const F2 ux = c.W2.v[1], uy = c.W2.v[2], dx = c.W4.v[1], dy = c.W4.v[2];
+        const F2 uxm = make_float2(__shfl_up_sync(kAll, ux.y, 1), ux.x), uym = make_float2(__shfl_up_sync(kAll, uy.y, 1), uy.x);
+        const F2 dxm = make_float2(__shfl_up_sync(kAll, dx.y, 1), dx.x), dym = make_float2(__shfl_up_sync(kAll, dy.y, 1), dy.x);
+        viscous_face2<0>(p.smag_on, k.nu, k.smag_c, k.inv_dx, k.inv_4dy, m1.v[0], own.v[0], m1.v[1], m1.v[2],
+                         own.v[1], own.v[2], add(ux, uxm), add(uy, uym), add(dx, dxm), add(dy, dym), F01.v[1],
+                         F01.v[2]);
+      }
 #pragma unroll
       for (int v = 0; v < 4; ++v) F2s[v] = v < NV ? __shfl_down_sync(0xffffffffu, F01.v[v].x, 1) : 0.f;  // face c0+2
       // The flux differences of both cells, each rounded on its own.
@@ -526,10 +582,15 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
             if (p.has_delta) vs.v[v] = delta_update(vs.v[v], k.delta, u.v[v]);
-            un.v[v] = rk_combine<float>(BLEND, k.g0, k.g1, u.v[v], vs.v[v], h == 0 ? dfx.v[v].x : dfx.v[v].y,
+            un.v[v] = rk_combine<float>(blend, k.g0, k.g1, u.v[v], vs.v[v], h == 0 ? dfx.v[v].x : dfx.v[v].y,
                                         h == 0 ? dfy.v[v].x : dfy.v[v].y, ncx, ncy);
           }
           un.v[3] = NV == 4 ? un.v[3] : 0.f;
+          if (drag) {
+            const float w0 = h == 0 ? own.v[0].x : own.v[0].y;
+            un.v[1] = drag_term(un.v[1], kdrag * w0, h == 0 ? own.v[1].x : own.v[1].y);
+            un.v[2] = drag_term(un.v[2], kdrag * w0, h == 0 ? own.v[2].x : own.v[2].y);
+          }
           if (p.floor_out) un.v[0] = N::lt(un.v[0], k.dfloor) ? k.dfloor : un.v[0];
           if (out[h]) {
             if (p.has_delta && Vo) store_cell<float, NV>(Vo + cell * NV, vs);
