@@ -379,9 +379,14 @@ def bench_ours(args, world, rank, local):
         compute_frac = flops / peak_tflops
         hbm_frac = gbs / hbm_peak
         bound = "fp64" if key == "f64" else ("fp32" if compute_frac >= hbm_frac else "hbm")
-        family = "stage_kernel_march" if res["tile"][0] in (26, 58, 90) else "stage_kernel_fast"
-        out = {"kernel": f"{family}<{'double' if w == 8 else 'float'},ppm4,roe,4> (RK3 stage 2, "
-                         f"tile {res['tile'][0]}x{res['tile'][1]})",
+        tx, ty = res["tile"]
+        if w == 4 and tx == 58:
+            # float32, two columns per lane: the packed-pair walk, row ring from 24 rows
+            kernel = f"stage_kernel_march_pk<ppm4,roe,4> ({'row ring, ' if ty >= 24 else ''}packed pairs"
+        else:
+            family = "stage_kernel_march" if tx in (26, 58, 90) else "stage_kernel_fast"
+            kernel = f"{family}<{'double' if w == 8 else 'float'},ppm4,roe,4> ("
+        out = {"kernel": f"{kernel}{', ' if kernel[-1] != '(' else ''}RK3 stage 2, tile {tx}x{ty})",
                "bound": bound, "achieved": round(flops, 4), "peak": round(peak_tflops, 4),
                "unit": "TFLOP/s", "frac": round(compute_frac, 4),
                "peak_source": f"{key.upper()} FMA pipe measured live by jx_probe_fma",
