@@ -83,48 +83,126 @@ def size_class(side):
 
 # Float32 precision guard. FP32_ERR holds, per (problem, reconstruction),
 # the worst float32-vs-float64 L1 density error measured over the three
-# Riemann solvers at end times FP32_ERR_TLIMS: row 0 the worst over sides 64,
-# 85, 128 and 256, row 1 at side 512 (GB300, `bench.py --precision-sweep`
-# and `--precision-sweep --n 512`). Two mechanisms make it grow, both
-# properties of the flows and limiters rather than of float32 arithmetic as
-# such: the shear layers (and, later, the waves) are chaotic, so any rounding
-# difference grows - a float64 run perturbed in its 15th digit drifts from
-# the unperturbed one by the same factors; and PPMX's smooth-extremum
-# limiter takes discrete branches (curvature signs, the 1e-12 relative
-# threshold, the extremum test on exactly equal neighbours) that these
-# symmetric set-ups put on exact ties, which rounding moves.
-FP32_ERR_TLIMS = (0.5, 1.0, 1.5, 2.0, 2.5, 3.0)
+# Riemann solvers, one row per side of FP32_ERR_SIDES and one column per end
+# time of FP32_ERR_TLIMS (GB300: `bench.py --precision-sweep` with
+# `--precision-tlims 0.1,0.2` and the default 0.5..3, each also with
+# `--n 512`; values rounded up to two digits). Two mechanisms make it grow,
+# both properties of the flows and limiters rather than of float32
+# arithmetic as such: the shear layers (and, later, the waves) are chaotic,
+# so any rounding difference grows - a float64 run perturbed in its 15th
+# digit drifts from the unperturbed one by the same factors; and PPMX's
+# smooth-extremum limiter takes discrete branches (curvature signs, the
+# 1e-12 relative threshold, the extremum test on exactly equal neighbours)
+# that these symmetric set-ups put on exact ties, which rounding moves -
+# most on the under-resolved shear layers of sides 64 and 85.
+FP32_ERR_SIDES = (64, 85, 128, 256, 512)
+FP32_ERR_TLIMS = (0.1, 0.2, 0.5, 1.0, 1.5, 2.0, 2.5, 3.0)
 FP32_ERR = {
-    ("kh", "dc"): ((1.3e-07, 1.8e-07, 3.8e-07, 8.7e-07, 1.6e-06, 2.5e-06),
-                   (3.8e-07, 6.1e-07, 1.4e-06, 1.9e-06, 3.3e-06, 8.7e-06)),
-    ("kh", "plm"): ((2.9e-07, 1.7e-06, 7.5e-06, 2.1e-05, 8.8e-05, 3.2e-04),
-                    (7.4e-07, 1.3e-06, 4.8e-06, 1.4e-05, 8.0e-05, 2.8e-04)),
-    ("kh", "ppm4"): ((5.4e-07, 2.3e-06, 2.1e-05, 3.8e-05, 7.7e-05, 2.5e-04),
-                     (8.5e-07, 2.2e-06, 1.4e-05, 4.7e-05, 1.7e-04, 7.0e-04)),
-    ("kh", "ppmx"): ((2.2e-04, 1.3e-03, 5.9e-03, 9.0e-03, 1.2e-02, 2.0e-02),
-                     (1.0e-06, 4.1e-06, 6.9e-05, 3.4e-04, 7.5e-04, 1.4e-03)),
-    ("kh", "wenoz"): ((3.7e-07, 1.4e-06, 1.1e-05, 2.8e-05, 1.3e-04, 5.1e-04),
-                      (7.0e-07, 1.4e-06, 6.5e-06, 1.6e-05, 4.0e-05, 2.2e-04)),
-    ("smooth", "dc"): ((6.9e-08, 6.9e-08, 8.1e-08, 7.6e-08, 7.5e-08, 7.3e-08),
-                       (7.5e-08, 7.3e-08, 7.8e-08, 7.7e-08, 8.0e-08, 8.5e-08)),
-    ("smooth", "plm"): ((1.2e-07, 1.5e-07, 1.7e-07, 1.7e-07, 1.8e-07, 2.1e-07),
-                        (1.6e-07, 1.9e-07, 2.1e-07, 2.3e-07, 2.4e-07, 2.4e-07)),
-    ("smooth", "ppm4"): ((5.0e-07, 5.3e-07, 5.1e-07, 8.8e-07, 1.1e-06, 7.3e-05),
-                         (6.4e-07, 6.8e-07, 8.5e-07, 7.6e-06, 2.2e-05, 3.5e-05)),
-    ("smooth", "ppmx"): ((5.5e-07, 1.2e-06, 1.1e-05, 2.0e-04, 3.0e-04, 3.6e-04),
-                         (6.4e-07, 7.0e-07, 9.3e-06, 1.4e-04, 1.8e-04, 2.3e-04)),
-    ("smooth", "wenoz"): ((2.2e-07, 3.8e-06, 7.5e-05, 5.2e-04, 5.4e-04, 7.5e-04),
-                          (2.7e-07, 3.2e-07, 3.6e-05, 2.8e-04, 4.3e-04, 5.1e-04)),
-    ("turbulence", "dc"): ((7.5e-08, 7.5e-08, 8.6e-08, 3.9e-07, 2.0e-07, 1.5e-07),
-                           (9.4e-08, 9.8e-08, 1.0e-07, 1.0e-07, 1.1e-07, 1.1e-07)),
-    ("turbulence", "plm"): ((1.3e-07, 1.5e-07, 1.7e-07, 1.6e-06, 8.9e-05, 1.3e-04),
-                            (1.8e-07, 2.0e-07, 2.2e-07, 2.3e-07, 2.4e-07, 2.8e-07)),
-    ("turbulence", "ppm4"): ((4.4e-07, 5.3e-07, 3.5e-06, 7.0e-05, 8.2e-05, 1.1e-04),
-                             (7.5e-07, 1.2e-06, 1.4e-06, 1.5e-06, 1.2e-06, 1.1e-06)),
-    ("turbulence", "ppmx"): ((5.4e-06, 3.7e-05, 1.1e-04, 1.7e-04, 2.3e-04, 3.0e-04),
-                             (6.4e-07, 7.6e-07, 1.2e-06, 3.5e-06, 6.6e-06, 1.1e-05)),
-    ("turbulence", "wenoz"): ((2.3e-07, 2.6e-07, 3.0e-07, 3.3e-07, 5.3e-07, 2.7e-06),
-                              (2.8e-07, 3.3e-07, 3.7e-07, 4.0e-07, 4.3e-07, 5.8e-06)),
+    ("kh", "dc"): (
+        (7.8e-08, 7.3e-08, 8.6e-08, 7.0e-08, 9.9e-08, 3.4e-07, 5.2e-07, 7.8e-07),  # 64
+        (6.9e-08, 6.9e-08, 8.1e-08, 8.9e-08, 1.5e-07, 4.0e-07, 7.9e-07, 9.8e-07),  # 85
+        (9.2e-08, 9.0e-08, 8.8e-08, 1.2e-07, 1.6e-07, 4.5e-07, 9.1e-07, 1.6e-06),  # 128
+        (1.5e-07, 1.6e-07, 1.3e-07, 1.8e-07, 3.8e-07, 8.8e-07, 1.6e-06, 2.5e-06),  # 256
+        (3.5e-07, 4.0e-07, 3.9e-07, 6.2e-07, 1.4e-06, 2.0e-06, 3.4e-06, 8.7e-06),  # 512
+    ),
+    ("kh", "plm"): (
+        (1.3e-07, 1.4e-07, 1.3e-07, 1.6e-07, 2.4e-07, 5.5e-07, 2.0e-06, 8.4e-06),  # 64
+        (1.3e-07, 1.4e-07, 1.4e-07, 2.3e-07, 4.4e-07, 8.3e-07, 7.1e-07, 1.1e-06),  # 85
+        (1.4e-07, 1.6e-07, 1.7e-07, 5.4e-07, 1.5e-06, 2.3e-06, 8.7e-06, 3.7e-05),  # 128
+        (2.1e-07, 2.4e-07, 2.9e-07, 1.7e-06, 7.5e-06, 2.2e-05, 8.8e-05, 3.3e-04),  # 256
+        (4.1e-07, 5.2e-07, 7.5e-07, 1.4e-06, 4.9e-06, 1.5e-05, 8.0e-05, 2.9e-04),  # 512
+    ),
+    ("kh", "ppm4"): (
+        (1.4e-07, 1.9e-07, 2.2e-07, 3.6e-07, 9.2e-07, 9.0e-07, 2.1e-06, 9.6e-06),  # 64
+        (1.8e-07, 2.3e-07, 3.1e-07, 6.3e-07, 1.9e-06, 2.4e-06, 3.5e-06, 6.6e-06),  # 85
+        (2.2e-07, 2.9e-07, 3.6e-07, 9.4e-07, 5.0e-06, 1.7e-05, 7.0e-05, 2.3e-04),  # 128
+        (3.3e-07, 4.2e-07, 5.5e-07, 2.4e-06, 2.1e-05, 3.8e-05, 7.8e-05, 2.6e-04),  # 256
+        (5.4e-07, 7.3e-07, 8.6e-07, 2.2e-06, 1.4e-05, 4.8e-05, 1.8e-04, 7.0e-04),  # 512
+    ),
+    ("kh", "ppmx"): (
+        (3.0e-06, 2.1e-05, 7.9e-05, 1.9e-04, 6.5e-04, 2.0e-03, 6.0e-03, 2.0e-02),  # 64
+        (7.0e-06, 4.3e-05, 2.3e-04, 1.3e-03, 5.9e-03, 9.1e-03, 1.3e-02, 1.5e-02),  # 85
+        (4.3e-07, 1.2e-06, 2.5e-06, 3.3e-05, 1.5e-04, 2.2e-04, 4.1e-04, 9.9e-04),  # 128
+        (3.6e-07, 6.1e-07, 1.9e-06, 1.3e-05, 7.9e-05, 2.1e-04, 5.3e-04, 1.7e-03),  # 256
+        (5.7e-07, 7.8e-07, 1.1e-06, 4.1e-06, 7.0e-05, 3.4e-04, 7.6e-04, 1.4e-03),  # 512
+    ),
+    ("kh", "wenoz"): (
+        (2.7e-07, 3.0e-07, 2.8e-07, 3.2e-07, 4.5e-07, 7.8e-07, 2.4e-06, 1.1e-05),  # 64
+        (2.1e-07, 2.6e-07, 2.9e-07, 4.3e-07, 9.5e-07, 1.7e-06, 1.9e-06, 3.4e-06),  # 85
+        (1.7e-07, 2.7e-07, 3.3e-07, 8.2e-07, 2.7e-06, 6.5e-06, 2.4e-05, 8.9e-05),  # 128
+        (2.3e-07, 2.9e-07, 3.7e-07, 1.5e-06, 1.1e-05, 2.8e-05, 1.4e-04, 5.2e-04),  # 256
+        (4.1e-07, 5.3e-07, 7.0e-07, 1.5e-06, 6.5e-06, 1.6e-05, 4.1e-05, 2.3e-04),  # 512
+    ),
+    ("smooth", "dc"): (
+        (5.7e-08, 6.6e-08, 6.4e-08, 6.6e-08, 6.6e-08, 7.1e-08, 6.8e-08, 6.7e-08),  # 64
+        (6.5e-08, 6.4e-08, 6.7e-08, 6.6e-08, 6.8e-08, 6.3e-08, 6.6e-08, 6.5e-08),  # 85
+        (6.3e-08, 5.7e-08, 6.1e-08, 6.6e-08, 7.9e-08, 7.7e-08, 7.5e-08, 6.7e-08),  # 128
+        (5.8e-08, 5.7e-08, 7.0e-08, 6.9e-08, 8.1e-08, 7.4e-08, 7.4e-08, 7.3e-08),  # 256
+        (6.5e-08, 7.5e-08, 7.6e-08, 7.3e-08, 7.9e-08, 7.7e-08, 8.1e-08, 8.6e-08),  # 512
+    ),
+    ("smooth", "plm"): (
+        (7.2e-08, 8.6e-08, 1.1e-07, 1.2e-07, 1.2e-07, 1.4e-07, 1.4e-07, 1.4e-07),  # 64
+        (8.1e-08, 9.2e-08, 9.7e-08, 1.2e-07, 1.3e-07, 1.3e-07, 1.6e-07, 1.7e-07),  # 85
+        (8.3e-08, 9.2e-08, 1.2e-07, 1.4e-07, 1.5e-07, 1.5e-07, 1.6e-07, 1.6e-07),  # 128
+        (8.9e-08, 1.2e-07, 1.3e-07, 1.5e-07, 1.7e-07, 1.7e-07, 1.9e-07, 2.2e-07),  # 256
+        (1.1e-07, 1.4e-07, 1.7e-07, 1.9e-07, 2.2e-07, 2.3e-07, 2.4e-07, 2.5e-07),  # 512
+    ),
+    ("smooth", "ppm4"): (
+        (1.6e-07, 2.0e-07, 2.6e-07, 2.9e-07, 3.1e-07, 2.8e-07, 2.8e-07, 4.1e-07),  # 64
+        (1.8e-07, 2.2e-07, 3.0e-07, 3.4e-07, 3.3e-07, 3.1e-07, 3.2e-07, 3.4e-07),  # 85
+        (2.1e-07, 2.6e-07, 3.6e-07, 4.0e-07, 3.9e-07, 4.8e-07, 8.7e-07, 1.3e-05),  # 128
+        (3.0e-07, 4.1e-07, 5.1e-07, 5.3e-07, 5.2e-07, 8.9e-07, 1.2e-06, 7.4e-05),  # 256
+        (4.0e-07, 5.4e-07, 6.5e-07, 6.8e-07, 8.5e-07, 7.6e-06, 2.3e-05, 3.6e-05),  # 512
+    ),
+    ("smooth", "ppmx"): (
+        (1.6e-07, 2.3e-07, 3.5e-07, 5.3e-07, 7.1e-06, 4.4e-05, 4.7e-05, 7.3e-05),  # 64
+        (1.9e-07, 2.6e-07, 3.8e-07, 1.2e-06, 5.4e-06, 3.7e-05, 9.9e-05, 1.7e-04),  # 85
+        (2.2e-07, 3.1e-07, 4.4e-07, 1.3e-06, 6.0e-06, 8.7e-05, 2.9e-04, 3.7e-04),  # 128
+        (3.0e-07, 4.0e-07, 5.5e-07, 6.7e-07, 1.2e-05, 2.0e-04, 3.1e-04, 3.3e-04),  # 256
+        (4.0e-07, 4.9e-07, 6.4e-07, 7.1e-07, 9.4e-06, 1.5e-04, 1.9e-04, 2.4e-04),  # 512
+    ),
+    ("smooth", "wenoz"): (
+        (1.1e-07, 1.3e-07, 1.6e-07, 4.1e-07, 2.9e-06, 4.7e-05, 8.7e-05, 4.5e-04),  # 64
+        (1.2e-07, 1.4e-07, 1.7e-07, 3.9e-06, 7.5e-05, 5.2e-04, 5.4e-04, 7.5e-04),  # 85
+        (1.3e-07, 1.5e-07, 2.0e-07, 2.4e-06, 4.9e-05, 2.5e-04, 3.8e-04, 6.1e-04),  # 128
+        (1.4e-07, 1.8e-07, 2.2e-07, 2.7e-07, 1.5e-05, 3.6e-04, 5.0e-04, 5.9e-04),  # 256
+        (1.7e-07, 2.1e-07, 2.7e-07, 3.3e-07, 3.7e-05, 2.9e-04, 4.3e-04, 5.2e-04),  # 512
+    ),
+    ("turbulence", "dc"): (
+        (5.5e-08, 6.7e-08, 6.6e-08, 7.4e-08, 7.7e-08, 3.9e-07, 2.1e-07, 1.6e-07),  # 64
+        (5.9e-08, 6.1e-08, 6.9e-08, 7.1e-08, 7.3e-08, 7.5e-08, 8.0e-08, 8.0e-08),  # 85
+        (6.0e-08, 6.1e-08, 6.3e-08, 7.2e-08, 7.4e-08, 7.0e-08, 8.4e-08, 8.6e-08),  # 128
+        (6.7e-08, 6.7e-08, 7.6e-08, 7.6e-08, 8.6e-08, 1.1e-07, 1.7e-07, 1.4e-07),  # 256
+        (8.4e-08, 8.3e-08, 9.5e-08, 9.8e-08, 1.1e-07, 1.1e-07, 1.2e-07, 1.2e-07),  # 512
+    ),
+    ("turbulence", "plm"): (
+        (6.9e-08, 8.3e-08, 1.1e-07, 1.2e-07, 1.3e-07, 1.3e-07, 1.4e-07, 1.5e-07),  # 64
+        (7.4e-08, 8.3e-08, 1.1e-07, 1.2e-07, 1.4e-07, 1.7e-06, 8.9e-05, 1.3e-04),  # 85
+        (7.9e-08, 8.9e-08, 1.2e-07, 1.3e-07, 1.5e-07, 1.6e-07, 1.8e-07, 2.8e-05),  # 128
+        (9.4e-08, 1.2e-07, 1.4e-07, 1.6e-07, 1.8e-07, 1.8e-07, 1.9e-07, 2.1e-07),  # 256
+        (1.3e-07, 1.5e-07, 1.8e-07, 2.1e-07, 2.3e-07, 2.4e-07, 2.5e-07, 2.8e-07),  # 512
+    ),
+    ("turbulence", "ppm4"): (
+        (1.2e-07, 1.6e-07, 2.1e-07, 2.4e-07, 2.8e-07, 3.0e-07, 3.6e-07, 6.0e-07),  # 64
+        (1.4e-07, 1.8e-07, 2.4e-07, 4.9e-07, 3.6e-06, 3.6e-06, 4.5e-06, 7.8e-06),  # 85
+        (1.8e-07, 2.3e-07, 3.1e-07, 3.7e-07, 4.6e-07, 7.0e-05, 8.3e-05, 1.1e-04),  # 128
+        (2.5e-07, 3.4e-07, 4.4e-07, 5.3e-07, 6.2e-07, 6.5e-07, 6.6e-07, 7.0e-07),  # 256
+        (3.6e-07, 4.7e-07, 7.6e-07, 1.3e-06, 1.4e-06, 1.5e-06, 1.3e-06, 1.1e-06),  # 512
+    ),
+    ("turbulence", "ppmx"): (
+        (2.2e-07, 5.6e-07, 5.4e-06, 3.8e-05, 1.2e-04, 1.8e-04, 2.3e-04, 3.0e-04),  # 64
+        (2.2e-07, 4.3e-07, 2.5e-06, 1.3e-05, 3.7e-05, 8.0e-05, 1.4e-04, 2.4e-04),  # 85
+        (2.2e-07, 3.2e-07, 6.4e-07, 2.1e-06, 9.1e-06, 3.0e-05, 4.6e-05, 6.2e-05),  # 128
+        (2.9e-07, 4.0e-07, 5.7e-07, 1.1e-05, 8.2e-06, 1.9e-05, 3.0e-05, 5.8e-05),  # 256
+        (3.8e-07, 4.9e-07, 6.5e-07, 7.7e-07, 1.2e-06, 3.6e-06, 6.7e-06, 1.2e-05),  # 512
+    ),
+    ("turbulence", "wenoz"): (
+        (9.9e-08, 1.3e-07, 1.5e-07, 1.8e-07, 2.2e-07, 2.4e-07, 2.6e-07, 2.6e-07),  # 64
+        (1.1e-07, 1.3e-07, 1.7e-07, 2.0e-07, 2.3e-07, 3.1e-07, 5.1e-07, 2.7e-06),  # 85
+        (1.2e-07, 1.5e-07, 1.8e-07, 2.2e-07, 2.6e-07, 2.7e-07, 5.3e-07, 1.8e-06),  # 128
+        (1.5e-07, 1.8e-07, 2.3e-07, 2.7e-07, 3.0e-07, 3.3e-07, 3.5e-07, 3.8e-07),  # 256
+        (1.9e-07, 2.2e-07, 2.8e-07, 3.4e-07, 3.7e-07, 4.1e-07, 4.4e-07, 5.9e-06),  # 512
+    ),
 }
 # Float32 is kept where the estimate stays at or under FP32_ERR_BAR, five
 # times below the 1e-5 L1 bar.
@@ -134,16 +212,19 @@ FP32_ERR_BAR = 2e-6
 def fp32_error_estimate(problem, reconstruct, side, tlim):
     """Estimated float32-vs-float64 L1 density error of a request: the worst
     measured error (FP32_ERR) at any end time up to the first measured one
-    at or past `tlim`, over the measured sides up to the request's (row 0
-    only for sides up to 256), times (side / 512)^2 above 512 (the measured
-    growth on the shear layer is about 2-3x per doubling of the side at a
-    fixed end time; 4x is the margin for unmeasured sides). None where
-    nothing was measured (end times past 3, unknown problems)."""
+    at or past `tlim`, on the measured sides next to the request's (the side
+    itself when measured, else the measured sides either side of it), times
+    (side / 512)^2 above 512 (the measured growth on the shear layer is
+    about 2-3x per doubling of the side at a fixed end time; 4x is the
+    margin for unmeasured sides). None where nothing was measured (end
+    times past 3, unknown problems)."""
     rows = FP32_ERR.get((problem, reconstruct))
     i = next((k for k, t in enumerate(FP32_ERR_TLIMS) if t >= tlim), None)
     if rows is None or i is None:
         return None
-    worst = max(rows[0][:i + 1]) if side <= 256 else max(max(rows[0][:i + 1]), max(rows[1][:i + 1]))
+    above = next((k for k, s in enumerate(FP32_ERR_SIDES) if s >= side), len(FP32_ERR_SIDES) - 1)
+    below = above if FP32_ERR_SIDES[above] <= side else max(above - 1, 0)
+    worst = max(max(rows[k][:i + 1]) for k in {below, above})
     return worst * max(1.0, side / 512.0) ** 2
 
 

@@ -163,13 +163,21 @@ def test_precision_guard_estimate():
     """The serving guard's float32 error estimate: measured values for the
     measured sides, side growth above 512, unknown past the measured end
     times, and the promotions it implies."""
-    from jathenax_gb300.serve import FP32_ERR, FP32_ERR_BAR, Request, fp32_error_estimate, served_dtype
-    assert fp32_error_estimate("kh", "dc", 128, 0.3) == FP32_ERR[("kh", "dc")][0][0]
-    # End times between measured ones take the worst up to the next one.
-    assert fp32_error_estimate("kh", "ppm4", 200, 1.2) == max(FP32_ERR[("kh", "ppm4")][0][:3])
-    # Sides above 256 include the 512 row; above 512 the estimate grows as side^2.
+    from jathenax_gb300.serve import (FP32_ERR, FP32_ERR_BAR, FP32_ERR_SIDES, FP32_ERR_TLIMS, Request,
+                                      fp32_error_estimate, served_dtype)
+    assert all(len(rows) == len(FP32_ERR_SIDES) and all(len(r) == len(FP32_ERR_TLIMS) for r in rows)
+               for rows in FP32_ERR.values())
+    kh_dc, kh_ppm4 = FP32_ERR[("kh", "dc")], FP32_ERR[("kh", "ppm4")]
+    # A measured side and end time: that measurement, or a worse one earlier.
+    assert fp32_error_estimate("kh", "dc", 128, 0.1) == kh_dc[2][0]
+    assert fp32_error_estimate("kh", "dc", 128, 0.2) == max(kh_dc[2][:2])
+    # End times between measured ones take the worst up to the next one; sides
+    # between measured ones the worse of the two either side.
+    assert fp32_error_estimate("kh", "ppm4", 200, 1.2) == max(max(kh_ppm4[2][:5]), max(kh_ppm4[3][:5]))
+    assert fp32_error_estimate("kh", "ppm4", 40, 0.3) == max(kh_ppm4[0][:3])
+    # Above 512 the estimate grows as side^2 from the 512 row.
     e512 = fp32_error_estimate("kh", "dc", 512, 2.0)
-    assert e512 == max(max(FP32_ERR[("kh", "dc")][0][:4]), max(FP32_ERR[("kh", "dc")][1][:4]))
+    assert e512 == max(kh_dc[4][:6])
     assert fp32_error_estimate("kh", "dc", 1024, 2.0) == pytest.approx(4 * e512)
     assert fp32_error_estimate("kh", "dc", 100, 3.5) is None
     assert fp32_error_estimate("kh", "unknown", 100, 1.0) is None
@@ -178,7 +186,10 @@ def test_precision_guard_estimate():
         return Request(rid=0, arrival=0.0, problem=problem, side=side, reconstruct=recon, rsolver="hlle",
                        tlim=tlim, dtype=dtype, seed=1)
 
-    assert served_dtype(req("kh", "ppmx", 64, 0.1)) == "float64"  # PPMX on the shear layer: always
+    assert served_dtype(req("kh", "ppmx", 64, 0.1)) == "float64"  # PPMX on an under-resolved shear layer
+    assert served_dtype(req("kh", "ppmx", 100, 0.1)) == "float64"  # next to side 85
+    assert served_dtype(req("kh", "ppmx", 200, 0.2)) == "float32"
+    assert served_dtype(req("kh", "ppmx", 200, 0.5)) == "float64"
     assert served_dtype(req("smooth", "dc", 2048, 3.0)) == "float32"
     assert served_dtype(req("kh", "dc", 1976, 2.24)) == "float64"
     assert served_dtype(req("kh", "dc", 1976, 2.24), guard=False) == "float32"
