@@ -58,8 +58,10 @@ def parse_args():
     p.add_argument("--n", type=int, default=None, help="grid side (default 4096; 1024 with --sweep)")
     p.add_argument("--no-fp32", action="store_true", help="skip the float32 line")
     p.add_argument("--only-fp32", action="store_true", help="time only the float32 state (profiling)")
-    p.add_argument("--cpu-sample", type=int, default=512, help="grid side of the CPU sample")
-    p.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU sample")
+    p.add_argument("--cpu-sample", type=int, default=None,
+                   help="grid side of the CPU (oracle) run (default: the benchmark grid, --n or 4096)")
+    p.add_argument("--cpu-steps", type=int, default=4,
+                   help="timed cycles of the CPU run in our line (the reference arm times min(--steps, 8))")
     p.add_argument("--no-patterns", action="store_true",
                    help="skip the batched / serving / precision measurements")
     p.add_argument("--serve-requests", type=int, default=100)
@@ -304,44 +306,30 @@ def run_precision(torch, _lib, Solve, U0, n, dtype, args, world, clocks=None):
                 dt=state.dt)
 
 
-def _oracle_cycles(n, steps, start_at=None):
-    """`steps` float64 oracle RK3 cycles (dt + 3 stages) on an n x n tanh KH state;
-    returns the seconds they took (after waiting for `start_at`, a wall-clock time)."""
-    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
-    from oracle import hydro_oracle as H
-    U = kelvin_helmholtz_tanh(n, n)
-    prev = np.inf
-    if start_at is not None:
-        time.sleep(max(0.0, start_at - time.time()))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        _, W = H.primitives(U, 1e-10)
-        dt = float(H.timestep(W, 1 / n, 1 / n, 1.0, 0.4, prev, 0.0, 1e30))
-        U = H.step(U, dt, 1 / n, 1 / n, 1.0, 1e-10, "rk3")
-        prev = dt
-    return time.perf_counter() - t0
-
-
 def cpu_baseline_sample(n, steps, procs=None):
-    """The float64 oracle (NumPy) on n x n samples of the workload, one independent
-    sample per host core in `spawn`ed processes that start together; the rate is
-    the total cell-updates over the slowest process's time."""
-    import multiprocessing as mp
-    from concurrent.futures import ProcessPoolExecutor
-    procs = procs or os.cpu_count() or 1
-    if procs == 1:
-        elapsed = [_oracle_cycles(n, steps)]
-    else:
-        # spawn: this process may already hold a CUDA context. A worker that
-        # dies raises BrokenProcessPool here instead of hanging the pool.
-        with ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as pool:
-            start_at = time.time() + 5.0  # every worker has imported NumPy by then
-            elapsed = list(pool.map(_oracle_cycles, [n] * procs, [steps] * procs, [start_at] * procs))
-    slowest = max(elapsed)
-    return dict(value=procs * n * n * steps / slowest, unit=METRIC, cores=procs, kind="port",
-                sample=f"float64 NumPy oracle, kelvin_helmholtz_tanh {n}x{n}, {steps} full RK3 cycles "
-                       f"(dt + 3 stages) in each of {procs} processes (one per host core)",
-                seconds=round(slowest, 2))
+    """The float64 oracle (NumPy) on the whole n x n tanh KH grid: one untimed,
+    then `steps` timed evolve cycles (dt + 3 RK stages), the grid split into row
+    slabs over `spawn`ed processes, one per host core (oracle.slab; bit for bit
+    the oracle's whole-grid cycles). The rate is the grid's cell-updates over
+    the slowest process's time."""
+    from jathenax_gb300.initial_conditions import kelvin_helmholtz_tanh
+    from oracle import slab
+    _, seconds, procs = slab.run(kelvin_helmholtz_tanh(n, n), cycles=steps, procs=procs, warm=1)
+    return dict(value=n * n * steps / seconds, unit=METRIC, cores=procs, kind="port",
+                sample=f"float64 NumPy oracle on the whole kelvin_helmholtz_tanh {n}x{n} grid, {steps} full "
+                       f"RK3 cycles (dt + 3 stages) after 1 untimed, in {procs} row slabs of about "
+                       f"{n // procs} rows (one process per host core, 3 halo rows a stage)",
+                seconds=round(seconds, 2))
+
+
+def workload_config(n, world):
+    """The benchmark workload, the same in both arms' lines."""
+    return {"workload": WORKLOAD.replace("4096x4096", f"{n}x{n}"), "nx": n, "ny": n, "nvar": 4,
+            "reconstruct": "ppm4", "rsolver": "roe", "integrator": "rk3", "cfl": 0.4,
+            "step": "one evolve cycle: CFL dt + 3 RK stages",
+            "l2": f"state {n * n * 4 * 8 / 1e6:.0f} MB" + (" > 129 MB L2 (no flush needed)"
+                                                           if n * n * 4 * 8 > 129e6 else ""),
+            "parallelism": f"replicas x{world}"}
 
 
 def bench_ours(args, world, rank, local):
@@ -425,11 +413,7 @@ def bench_ours(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(r64["ms"] / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD.replace("4096x4096", f"{n}x{n}"), "nx": n, "ny": n, "nvar": 4,
-                   "reconstruct": "ppm4", "rsolver": "roe", "integrator": "rk3", "cfl": 0.4,
-                   "step": "one evolve cycle: CFL dt + 3 fused RK stages (CUDA graph replay)",
-                   "l2": f"state {cells * 4 * 8 / 1e6:.0f} MB > 129 MB L2 (no flush needed)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(n, world),
         "roofline": roofline(r64, w64, probe64, "f64"),
         "e2e": r64["e2e"],
         "gpu_launches": 4 * args.steps,  # per step: begin-step + 3 stage kernels
@@ -441,7 +425,7 @@ def bench_ours(args, world, rank, local):
                         "roofline": roofline(r32, 4, probe32, "f32"), "e2e": r32["e2e"],
                         "gpu_launches": 4 * args.steps}
     if rank == 0 and world == 1 and args.cpu_steps > 0:
-        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_sample or n, args.cpu_steps)
     if rank == 0 and world == 1 and not args.no_patterns:
         line["batched"] = bench_batched(torch)
         line["serving"] = bench_serving(torch, args.serve_requests)
@@ -793,17 +777,18 @@ def bench_reference(args, world, rank):
     """The reference algorithm's CPU path (the float64 oracle port) on host cores."""
     if rank != 0:
         return None
-    base = cpu_baseline_sample(args.cpu_sample, max(1, min(args.steps, args.cpu_steps)))
-    steps = base.pop("seconds")
+    n = args.cpu_sample or args.n or 4096
+    base = cpu_baseline_sample(n, max(1, min(args.steps, 8)))
+    seconds = base.pop("seconds")
     return {
         "impl": "reference", "metric": METRIC, "value": round(base["value"], 1), "unit": METRIC,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_side": args.cpu_sample},
+        "config": workload_config(n, world),
         "cpu_baseline": dict(base),
         "e2e": {"value": round(base["value"], 1), "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "seconds": steps,
+        "seconds": seconds,
     }
 
 
