@@ -443,6 +443,10 @@ def summary(line):
         r = line["fp32"]["roofline"]
         out["f32"] = {"cell_updates_per_s": line["fp32"]["value"], "e2e": round(line["fp32"]["e2e"]["value"], 1),
                       "stage_ms": r["stage_ms"], "hbm_frac": r["hbm"]["frac"]}
+    cpu = line.get("cpu_baseline")
+    if cpu:
+        out["cpu_baseline"] = {"cell_updates_per_s": round(cpu["value"], 1), "cores": cpu["cores"],
+                               "f64_e2e_over_cpu": round(line["e2e"]["value"] / cpu["value"], 1)}
     b = line.get("batched")
     if b:
         out["batched"] = {k: b[k] for k in ("speedup", "batched_fp32_solves_per_s", "serial_fp64_solves_per_s",
