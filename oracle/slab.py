@@ -144,7 +144,9 @@ def run(U0, cycles, procs=None, warm=0, cs=1.0, dfloor=1e-10, cfl=0.4, recon="pp
                                                     mins_path, results), daemon=True) for r in range(procs)]
         for w in workers:
             w.start()
-        got, deadline = {}, time.monotonic() + BARRIER_TIMEOUT_S
+        # A backstop only: a worker that dies is seen by its exit code, and one
+        # left waiting at a barrier gives up after BARRIER_TIMEOUT_S and reports.
+        got, deadline = {}, time.monotonic() + BARRIER_TIMEOUT_S * (warm + cycles + 2)
         while len(got) < procs:
             try:
                 rank, cur, value = results.get(timeout=1.0)
