@@ -45,7 +45,7 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # Thread instructions per cell of the float32 marching stage (ppm4+roe, 4
 # variables, packed-pair walk with the row ring): smsp__inst_executed.sum x
 # 32 / cells of one launch.
-STAGE_INST_PER_CELL_F32 = 124.83e6 * 32 / 3072**2
+STAGE_INST_PER_CELL_F32 = 125.14e6 * 32 / 3072**2
 STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (552.06e6 + 236.47e6) / 4096**2}
 
 
@@ -369,8 +369,10 @@ def bench_ours(args, world, rank, local):
         bound = "fp64" if key == "f64" else ("fp32" if compute_frac >= hbm_frac else "hbm")
         tx, ty = res["tile"]
         if w == 4 and tx == 58:
-            # float32, two columns per lane: the packed-pair walk, row ring from 24 rows
-            kernel = f"stage_kernel_march_pk<ppm4,roe,4> ({'row ring, ' if ty >= 24 else ''}packed pairs"
+            # float32, two columns per lane: the packed-pair walk; from 24 rows the
+            # row-ring kernel at 112 registers with the x sweep first
+            kernel = (f"stage_kernel_march_pk_x<roe,4,blend> (PPM4, row ring, x sweep first, 112 registers, packed pairs"
+                      if ty >= 24 else "stage_kernel_march_pk<ppm4,roe,4,blend> (packed pairs")
         else:
             family = "stage_kernel_march" if tx in (26, 58, 90) else "stage_kernel_fast"
             kernel = f"{family}<{'double' if w == 8 else 'float'},ppm4,roe,4> ("

@@ -412,7 +412,10 @@ struct ColumnPair {
 // FORM: 0 = generic (viscosity, Smagorinsky, drag and the blend flag read at
 // run time; no SGS stress), 1 = lean plain, 2 = lean blend (the MarchForm
 // values).
-template <int RECON, int RS, int NV, int FORM, bool RING>
+// XFIRST: run each row's x sweep ahead of its y sweep (fewer values live
+// across the row: the single-solve PPM4 ring kernel fits 112 registers
+// without spills only this way). Either order gives the same bits.
+template <int RECON, int RS, int NV, int FORM, bool RING, bool XFIRST = false>
 __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, int ntiles, float4* ring) {
   using N = Num<float>;
   const StageConsts<float>& k = stage_consts<float>(p);
@@ -502,28 +505,11 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
 #pragma unroll
       for (int h = 0; h < 2; ++h) next[h] = load_cell<float, NV>(U + (row + gx[h]) * NV);
     }
-    // ---- y sweep of both columns -------------------------------------------
-    PCell Ay1 = c.Ay2;
-    if constexpr (RECON == JX_PPM4 || RECON == JX_PPMX)
-      if (kSteady || it >= 3) Ay1 = faces2<RECON, NV>(c.W3, c.W2, c.W1, c.W0);
-    PCell lo = c.hy3, hi = c.hy3;
-    if (kSteady || it >= 4) edges2<RECON, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1, k.dfloor, lo, hi);
-    PCell Fy2 = c.Fy3;
-    if (kSteady || it >= 5) {
-      Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
-      if (visc) {
-        // Transverse x sums (row j-2 + row j-3) at the columns either side;
-        // a neighbour lane's sum is the same number it formed itself.
-        const F2 Sx = add(c.W2.v[1], c.W3.v[1]), Sy = add(c.W2.v[2], c.W3.v[2]);
-        const float sxm = __shfl_up_sync(kAll, Sx.y, 1), sym = __shfl_up_sync(kAll, Sy.y, 1);      // column c0-1
-        const float sxp = __shfl_down_sync(kAll, Sx.x, 1), syp = __shfl_down_sync(kAll, Sy.x, 1);  // column c0+2
-        viscous_face2<1>(p.smag_on, k.nu, k.smag_c, k.inv_dy, k.inv_4dx, c.W3.v[0], c.W2.v[0], c.W3.v[1], c.W3.v[2],
-                         c.W2.v[1], c.W2.v[2], make_float2(Sx.y, sxp), make_float2(Sy.y, syp),
-                         make_float2(sxm, Sx.x), make_float2(sym, Sy.x), Fy2.v[1], Fy2.v[2]);
-      }
-    }
-    if (kSteady) {
-      // ---- x sweep of row r = j-3 across the lanes -------------------------
+    // ---- x sweep of row r = j-3 across the lanes (dfx: the two cells' x flux
+    // differences); with XFIRST ahead of the y sweep, else just before the
+    // combine ---------------------------------------------------------------
+    PCell dfx;
+    auto x_sweep = [&] {
       const PCell& own = c.W3;                           // columns (c0, c0+1)
       const PCell L = shfl_up<NV>(own, 1);               // (c0-2, c0-1)
       const PCell R = shfl_down<NV>(own, 1);             // (c0+2, c0+3)
@@ -556,12 +542,37 @@ __device__ __forceinline__ void march_tile_pk(const StageParams& p, int tile, in
       for (int v = 0; v < 4; ++v) F2s[v] = v < NV ? __shfl_down_sync(0xffffffffu, F01.v[v].x, 1) : 0.f;  // face c0+2
       // The flux differences of both cells, each rounded on its own.
       const PCell F12 = straddle<NV>(F01, F2s);
-      PCell dfx, dfy;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        dfx.v[v] = sub(F12.v[v], F01.v[v]);
-        dfy.v[v] = sub(Fy2.v[v], c.Fy3.v[v]);
+      for (int v = 0; v < 4; ++v) dfx.v[v] = sub(F12.v[v], F01.v[v]);
+    };
+    if constexpr (XFIRST)
+      if (kSteady) x_sweep();
+    // ---- y sweep of both columns -------------------------------------------
+    PCell Ay1 = c.Ay2;
+    if constexpr (RECON == JX_PPM4 || RECON == JX_PPMX)
+      if (kSteady || it >= 3) Ay1 = faces2<RECON, NV>(c.W3, c.W2, c.W1, c.W0);
+    PCell lo = c.hy3, hi = c.hy3;
+    if (kSteady || it >= 4) edges2<RECON, NV>(c.W4, c.W3, c.W2, c.W1, c.W0, c.Ay2, Ay1, k.dfloor, lo, hi);
+    PCell Fy2 = c.Fy3;
+    if (kSteady || it >= 5) {
+      Fy2 = face_flux2<RS, 1, NV>(c.hy3, lo, gas);
+      if (visc) {
+        // Transverse x sums (row j-2 + row j-3) at the columns either side;
+        // a neighbour lane's sum is the same number it formed itself.
+        const F2 Sx = add(c.W2.v[1], c.W3.v[1]), Sy = add(c.W2.v[2], c.W3.v[2]);
+        const float sxm = __shfl_up_sync(kAll, Sx.y, 1), sym = __shfl_up_sync(kAll, Sy.y, 1);      // column c0-1
+        const float sxp = __shfl_down_sync(kAll, Sx.x, 1), syp = __shfl_down_sync(kAll, Sy.x, 1);  // column c0+2
+        viscous_face2<1>(p.smag_on, k.nu, k.smag_c, k.inv_dy, k.inv_4dx, c.W3.v[0], c.W2.v[0], c.W3.v[1], c.W3.v[2],
+                         c.W2.v[1], c.W2.v[2], make_float2(Sx.y, sxp), make_float2(Sy.y, syp),
+                         make_float2(sxm, Sx.x), make_float2(sym, Sy.x), Fy2.v[1], Fy2.v[2]);
       }
+    }
+    if (kSteady) {
+      if constexpr (!XFIRST) x_sweep();
+      const PCell& own = c.W3;
+      PCell dfy;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) dfy.v[v] = sub(Fy2.v[v], c.Fy3.v[v]);
       const int r = j - 3;
       if (r < p.ny) {
         const size_t row = (size_t)r * p.nx;
