@@ -46,7 +46,7 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # variables, packed-pair walk with the row ring): smsp__inst_executed.sum x
 # 32 / cells of one launch.
 STAGE_INST_PER_CELL_F32 = 125.14e6 * 32 / 3072**2
-STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (552.06e6 + 236.47e6) / 4096**2}
+STAGE_TRAFFIC_BYTES_PER_CELL = {"f64": (1075.99e6 + 509.14e6) / 4096**2, "f32": (552.01e6 + 236.64e6) / 4096**2}
 
 
 def parse_args():
