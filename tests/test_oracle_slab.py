@@ -39,3 +39,9 @@ def test_slab_bounds_cover_the_grid():
         bounds = [slab.slab_bounds(n, procs, r) for r in range(procs)]
         assert bounds[0][0] == 0 and bounds[-1][1] == n
         assert all(a[1] == b[0] for a, b in zip(bounds, bounds[1:]))
+
+
+def test_a_failing_worker_is_reported_not_waited_for():
+    U0 = kelvin_helmholtz_tanh(24, 24)
+    with pytest.raises(RuntimeError, match="failed"):
+        slab.run(U0, cycles=1, procs=2, recon="no-such-method")
