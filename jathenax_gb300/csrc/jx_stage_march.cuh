@@ -550,9 +550,10 @@ __global__ void __launch_bounds__(32, RECON >= JX_PPMX ? 12 : 16) stage_kernel_m
 // without spills (the y sweep first spilled 20 bytes at 112 and took 0.328
 // ms). Measured at 4096²: 0.2569-0.2589 ms per stage against 0.2645 ms for
 // the y-first walk at 122 registers, the same bits; ncu at 3072² shows the
-// same 16 resident blocks per SM (its register limit stays at 16, shared
-// memory allows 17), the same instructions per cell, and issue 69.2 % of
-// cycles against 67.3 %: the gain is the schedule, not occupancy. The x
+// same 16 resident blocks per SM (registers are allocated per scheduler, 16 K
+// each: 112 or 122 a thread both leave room for 4 warps, 5 need 96 or fewer,
+// which spills), the same instructions per cell, and issue 69.2 % of cycles
+// against 67.3 %: the gain is the schedule, not occupancy. The x
 // sweep first at 122 registers changed nothing, and short tiles (no ring)
 // spill at 112. The register count is a template argument because nvcc
 // accepts __launch_bounds__ beside __maxnreg__ only in that form (without
